@@ -1,0 +1,320 @@
+"""cusat_gb300 -- GB300-native receive-side FEC path for DVB-S2/S2X.
+
+Soft demapping with deinterleave, layered offset min-sum LDPC decoding on
+int16 LLRs with a syndrome early exit, and the BCH syndrome check, as
+hand-written sm_103a CUDA kernels behind the C ABI of include/cusat_fec.h.
+This module is the Python host side of that ABI.  Its classes keep the names,
+arguments and result conventions of the reference's C++ classes for the path:
+
+  ldpc_decode_cuda  lib/cusat_dsp/cuda/ldpc_decode_kernel.cuh:22-107
+  ldpc_decode       lib/cusat_dsp/ldpc_decode.h:22-69
+  demapper_cuda     lib/cusat_dsp/cuda/demapper_kernel.cuh:23-89
+  bch_check_cuda    lib/cusat_dsp/cuda/bch_check_kernel.cuh:9-24
+
+plus ``rx_fec`` (one MODCOD's fused demap -> decode -> BCH chain).
+
+Device buffers are torch CUDA tensors (or raw device addresses as int);
+host buffers are numpy arrays.  Streams are torch.cuda.Stream objects, raw
+cudaStream_t values as int, or None (legacy default stream).  There is no
+CPU fallback: without the built library or a GPU every call raises.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import CusatError
+from .enums import *  # noqa: F401,F403
+from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
+
+__all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec",
+           "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
+           "CusatError", "library_path"]
+
+
+def library_path():
+    return _capi.LIB_PATH
+
+
+def _addr(x):
+    """Device/host address of a torch tensor, numpy array, int or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    if hasattr(s, "cuda_stream"):
+        return s.cuda_stream
+    raise TypeError(f"not a stream: {type(s)}")
+
+
+def _host(a, dtype, n):
+    a = np.ascontiguousarray(a, dtype)
+    if a.size < n:
+        raise ValueError(f"host buffer holds {a.size} elements, {n} needed")
+    return a
+
+
+def _info(fn, handle, n):
+    out = np.zeros(n, np.int32)
+    _capi.check(fn(handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+    return [int(v) for v in out]
+
+
+def code_info(framesize, rate):
+    """Dimensions of the (framesize, rate) code: n_ldpc, k_ldpc, k_bch, n_bch,
+    t, bch_degree, q, n_steps, lanes, cmax, edges, cnt_max."""
+    L = _capi.lib()
+    out = np.zeros(12, np.int32)
+    _capi.check(L.cusat_code_info(framesize, rate, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+    keys = ["n_ldpc", "k_ldpc", "k_bch", "n_bch", "t", "bch_degree", "q", "n_steps", "lanes", "cmax",
+            "edges", "cnt_max"]
+    return dict(zip(keys, (int(v) for v in out)))
+
+
+def modcod_info(modulation, rate, framesize):
+    """Constellation points (complex64, by label), interleaver column offsets
+    and frame geometry of a MODCOD."""
+    L = _capi.lib()
+    pts = np.zeros(2 * 256, np.float32)
+    col = np.zeros(8, np.uint32)
+    out = np.zeros(6, np.int32)
+    _capi.check(L.cusat_modcod_info(modulation, rate, framesize, pts.ctypes.data, col.ctypes.data,
+                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+    n_mod, n_points, fec_len, xfec, il, kind = (int(v) for v in out)
+    p = pts[:2 * n_points]
+    return {"n_mod": n_mod, "n_points": n_points, "fecframe_len": fec_len, "xfecframe_len": xfec,
+            "interleaved_len": il, "kind": kind, "points": (p[0::2] + 1j * p[1::2]).astype(np.complex64),
+            "col_offset": col}
+
+
+def capped_llr_gain(modulation, rate, framesize, llr_gain):
+    return float(_capi.lib().cusat_modcod_capped_llr_gain(modulation, rate, framesize, llr_gain))
+
+
+def encode_frames(framesize, rate, msg):
+    """BCH + LDPC encode k_bch/8-byte messages into n_ldpc/8-byte codewords."""
+    ci = code_info(framesize, rate)
+    msg = np.ascontiguousarray(msg, np.uint8).reshape(-1, ci["k_bch"] // 8)
+    cw = np.zeros((msg.shape[0], ci["n_ldpc"] // 8), np.uint8)
+    _capi.check(_capi.lib().cusat_gen_encode(framesize, rate, msg.ctypes.data, cw.ctypes.data, msg.shape[0]))
+    return cw
+
+
+def map_frames(modulation, rate, framesize, cw):
+    """Interleave + map codewords to symbols: float32 [B, xfecframe_len * 2]."""
+    mi = modcod_info(modulation, rate, framesize)
+    cw = np.ascontiguousarray(cw, np.uint8).reshape(-1, mi["fecframe_len"] // 8)
+    sym = np.zeros((cw.shape[0], mi["xfecframe_len"] * 2), np.float32)
+    _capi.check(_capi.lib().cusat_gen_map(modulation, rate, framesize, cw.ctypes.data, cw.shape[0],
+                                          sym.ctypes.data))
+    return sym
+
+
+class ldpc_decode_cuda:
+    """Layered min-sum LDPC decoder (reference cuda::ldpc_decode_cuda).
+
+    ``decode_launch_async`` is the asynchronous device path; ``decode_batch``
+    and ``decode_batch_d2h`` are the synchronous host-result paths.  Trials
+    are max_trials - iterations used, or -1 when not converged."""
+
+    def __init__(self, framesize, rate, max_trials=25, max_batch=64):
+        L = _capi.lib()
+        h = ctypes.c_void_p()
+        _capi.check(L.cusat_ldpc_decoder_create(framesize, rate, max_trials, max_batch, ctypes.byref(h)))
+        self._h = h
+        info = _info(L.cusat_ldpc_decoder_info, h, 8)
+        self.framesize, self.rate = framesize, rate
+        self._n, self._k, self._kb, self.q, self.n_steps, self.max_trials, self.max_batch, self.lanes = info
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_ldpc_decoder_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def n_bits(self):
+        return self._n
+
+    def k_bits(self):
+        return self._k
+
+    def k_bytes(self):
+        return self._kb
+
+    def decode_launch_async(self, soft_in, batch_size, stream=None, hard_out=None, result_out=None):
+        _capi.check(_capi.lib().cusat_ldpc_decode_launch(self._h, _addr(soft_in), batch_size, _stream(stream),
+                                                          _addr(hard_out), _addr(result_out)))
+
+    def results(self, batch_size):
+        hard = np.zeros((batch_size, self._kb), np.uint8)
+        trials = np.zeros(batch_size, np.int32)
+        _capi.check(_capi.lib().cusat_ldpc_decoder_results(self._h, hard.ctypes.data, trials.ctypes.data,
+                                                           batch_size))
+        return hard, trials
+
+    def decode_batch(self, soft_in, batch_size=None, stream=None):
+        soft = np.ascontiguousarray(soft_in, np.int16).reshape(-1, self._n)
+        b = soft.shape[0] if batch_size is None else batch_size
+        hard = np.zeros((b, self._kb), np.uint8)
+        trials = np.zeros(b, np.int32)
+        _capi.check(_capi.lib().cusat_ldpc_decode_batch(self._h, soft.ctypes.data, hard.ctypes.data,
+                                                        trials.ctypes.data, b, _stream(stream)))
+        return hard, trials
+
+    def decode_batch_d2h(self, soft_in_dev, batch_size, stream=None):
+        hard = np.zeros((batch_size, self._kb), np.uint8)
+        trials = np.zeros(batch_size, np.int32)
+        _capi.check(_capi.lib().cusat_ldpc_decode_batch_d2h(self._h, _addr(soft_in_dev), hard.ctypes.data,
+                                                            trials.ctypes.data, batch_size, _stream(stream)))
+        return hard, trials
+
+
+class ldpc_decode(ldpc_decode_cuda):
+    """Standalone decoder (reference cusat_dsp::ldpc_decode): owns a stream."""
+
+    def __init__(self, framesize, rate, max_trials=25, cuda_max_batch=64):
+        super().__init__(framesize, rate, max_trials, cuda_max_batch)
+        import torch
+        self._stream = torch.cuda.Stream()
+
+    def cuda_stream(self):
+        return self._stream
+
+    def n_bytes(self):
+        return self._n // 8
+
+    def decode_batch_cuda(self, soft_in, batch_size=None):
+        return self.decode_batch(soft_in, batch_size, self._stream)
+
+    def decode_batch_cuda_d2h(self, soft_in_dev, batch_size):
+        return self.decode_batch_d2h(soft_in_dev, batch_size, self._stream)
+
+
+class demapper_cuda:
+    """Soft demapper + deinterleaver (reference cuda::demapper_cuda)."""
+
+    def __init__(self, constellation, rate, framesize, max_batch=64):
+        L = _capi.lib()
+        h = ctypes.c_void_p()
+        _capi.check(L.cusat_demapper_create(constellation, rate, framesize, max_batch, ctypes.byref(h)))
+        self._h = h
+        self._fec, self._xfec, self._nmod, self._il = _info(L.cusat_demapper_info, h, 4)
+        self.max_batch = max_batch
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_demapper_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def fecframe_len(self):
+        return self._fec
+
+    def xfecframe_len(self):
+        return self._xfec
+
+    def n_mod(self):
+        return self._nmod
+
+    def capped_llr_gain(self, llr_gain):
+        return float(_capi.lib().cusat_demapper_capped_llr_gain(self._h, llr_gain))
+
+    def soft_out_dev(self):
+        """Device address of the internal LLR buffer."""
+        return int(_capi.lib().cusat_demapper_soft_out_dev(self._h))
+
+    def demap_launch(self, sym_dev, batch_size, noise_var, llr_gain, soft_out_dev=None, stream=None):
+        _capi.check(_capi.lib().cusat_demap_launch(self._h, _addr(sym_dev), batch_size, noise_var, llr_gain,
+                                                   _addr(soft_out_dev), _stream(stream)))
+
+    def demap_batch_async(self, sym_in_host, batch_size, noise_var, llr_gain, stream=None):
+        sym = _host(sym_in_host, np.float32, batch_size * self._xfec * 2)
+        self._keep = sym
+        _capi.check(_capi.lib().cusat_demap_batch_async(self._h, sym.ctypes.data, batch_size, noise_var,
+                                                        llr_gain, _stream(stream)))
+
+    def demap_batch(self, sym_in_host, batch_size, noise_var, llr_gain):
+        sym = _host(sym_in_host, np.float32, batch_size * self._xfec * 2)
+        _capi.check(_capi.lib().cusat_demap_batch(self._h, sym.ctypes.data, batch_size, noise_var, llr_gain))
+
+
+class bch_check_cuda:
+    """BCH syndrome check (reference cuda::bch_check_cuda)."""
+
+    def __init__(self, flat_lut, gen_poly, gen_degree, n_bytes):
+        lut = np.ascontiguousarray(flat_lut, np.uint64).reshape(256 * 4)
+        gen = np.ascontiguousarray(gen_poly, np.uint64).reshape(4)
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_bch_checker_create(lut.ctypes.data, gen.ctypes.data, gen_degree, n_bytes,
+                                                         ctypes.byref(h)))
+        self._h = h
+        self.degree = gen_degree
+
+    @classmethod
+    def for_code(cls, framesize, rate):
+        self = cls.__new__(cls)
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_bch_checker_create_for_code(framesize, rate, ctypes.byref(h)))
+        self._h = h
+        self.degree = code_info(framesize, rate)["bch_degree"]
+        return self
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_bch_checker_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def n_bytes(self):
+        return int(_capi.lib().cusat_bch_checker_n_bytes(self._h))
+
+    def check_async(self, codewords_dev, valid_out_dev, batch_size, stream=None, rem_out_dev=None):
+        _capi.check(_capi.lib().cusat_bch_check_launch(self._h, _addr(codewords_dev), _addr(valid_out_dev),
+                                                       _addr(rem_out_dev), batch_size, _stream(stream)))
+
+
+class rx_fec:
+    """One MODCOD's receive chain: fused demap + deinterleave + LDPC decode,
+    then the BCH check (replaces rx_fec_chain::launch_slot_gpu's launch
+    sequence, lib/cusat_dsp/rx_fec_chain.cc:361-505)."""
+
+    def __init__(self, constellation, rate, framesize, max_trials=25, max_batch=64):
+        L = _capi.lib()
+        h = ctypes.c_void_p()
+        _capi.check(L.cusat_rx_fec_create(constellation, rate, framesize, max_trials, max_batch,
+                                          ctypes.byref(h)))
+        self._h = h
+        self.xfec, self.n_bits, self.k_bits, self.k_bytes, self.k_bch, self.n_mod = _info(L.cusat_rx_fec_info,
+                                                                                          h, 6)
+        self.max_trials, self.max_batch = max_trials, max_batch
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_rx_fec_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def capped_llr_gain(self, llr_gain):
+        return float(_capi.lib().cusat_rx_fec_capped_llr_gain(self._h, llr_gain))
+
+    def launch(self, sym_dev, batch_size, noise_var, llr_gain, hard_out, trials_out, bch_valid_out=None,
+               stream=None):
+        _capi.check(_capi.lib().cusat_rx_fec_launch(self._h, _addr(sym_dev), batch_size, noise_var, llr_gain,
+                                                    _addr(hard_out), _addr(trials_out), _addr(bch_valid_out),
+                                                    _stream(stream)))

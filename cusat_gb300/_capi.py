@@ -1,0 +1,101 @@
+"""ctypes binding of the C ABI (include/cusat_fec.h).
+
+Loads the in-tree ``cusat_gb300/_lib/libcusat_fec.so``.  There is no CPU
+fallback: if the library is missing or was built for another machine, the
+first use raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libcusat_fec.so")
+
+_c_int_p = ctypes.POINTER(ctypes.c_int32)
+_lib = None
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "cusat_last_error": (ctypes.c_char_p, []),
+    "cusat_ldpc_decoder_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_ldpc_decoder_destroy": (None, [ctypes.c_void_p]),
+    "cusat_ldpc_decoder_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_ldpc_decode_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
+    "cusat_ldpc_decode_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_int, ctypes.c_void_p]),
+    "cusat_ldpc_decode_batch_d2h": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "cusat_ldpc_decoder_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_int]),
+    "cusat_demapper_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_demapper_destroy": (None, [ctypes.c_void_p]),
+    "cusat_demapper_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_demapper_capped_llr_gain": (ctypes.c_float, [ctypes.c_void_p, ctypes.c_float]),
+    "cusat_demapper_soft_out_dev": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "cusat_demap_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]),
+    "cusat_demap_batch_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                               ctypes.c_float, ctypes.c_void_p]),
+    "cusat_demap_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                         ctypes.c_float]),
+    "cusat_bch_checker_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint,
+                                                ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_bch_checker_create_for_code": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
+                                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_bch_checker_destroy": (None, [ctypes.c_void_p]),
+    "cusat_bch_checker_n_bytes": (ctypes.c_uint, [ctypes.c_void_p]),
+    "cusat_bch_check_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_int, ctypes.c_void_p]),
+    "cusat_rx_fec_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_rx_fec_destroy": (None, [ctypes.c_void_p]),
+    "cusat_rx_fec_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_rx_fec_capped_llr_gain": (ctypes.c_float, [ctypes.c_void_p, ctypes.c_float]),
+    "cusat_rx_fec_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    "cusat_code_info": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_int_p]),
+    "cusat_gen_encode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int]),
+    "cusat_gen_map": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.c_void_p]),
+    "cusat_modcod_info": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                         ctypes.c_void_p, _c_int_p]),
+    "cusat_modcod_capped_llr_gain": (ctypes.c_float, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                      ctypes.c_float]),
+}
+
+
+class CusatError(RuntimeError):
+    """A C-ABI call returned an error code."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"cusat error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() "
+                              f"(or python cusat_gb300/build.py) on this machine first")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise CusatError(rc, lib().cusat_last_error().decode())
+    return rc
+
+
+def exported_symbols():
+    return list(_SIGS)

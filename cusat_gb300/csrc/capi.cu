@@ -1,0 +1,730 @@
+// C ABI (include/cusat_fec.h) over the FEC kernels.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cusat_fec.h"
+#include "host.h"
+#include "kernels.h"
+#include "ldpc_kernel.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return CUSAT_ERR_CUDA;
+}
+
+#define CU(call, what)                          \
+    do {                                        \
+        cudaError_t e_ = (call);                \
+        if (e_ != cudaSuccess)                  \
+            return cuda_fail(e_, what);         \
+    } while (0)
+
+int require_device(int* dev)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(CUSAT_ERR_NO_DEVICE, "no CUDA device");
+    e = cudaGetDevice(dev);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    return CUSAT_OK;
+}
+
+// Device copy of a code plan (one allocation).
+struct DevPlan {
+    void* blob = nullptr;
+    cusat::DevCode code{};
+};
+
+int upload_plan(const cusat::CodePlan& p, DevPlan* d)
+{
+    const size_t n_circ = p.circ.size() * 4, n_cnt = p.cnt.size(), n_sched = p.sched.size() * 2,
+                 n_conf = p.step_conf.size();
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_circ = 0, o_cnt = al(n_circ), o_sched = o_cnt + al(n_cnt), o_conf = o_sched + al(n_sched);
+    const size_t total = o_conf + al(n_conf);
+    std::vector<unsigned char> h(total, 0);
+    memcpy(&h[o_circ], p.circ.data(), n_circ);
+    memcpy(&h[o_cnt], p.cnt.data(), n_cnt);
+    memcpy(&h[o_sched], p.sched.data(), n_sched);
+    memcpy(&h[o_conf], p.step_conf.data(), n_conf);
+    CU(cudaMalloc(&d->blob, total), "cudaMalloc(plan)");
+    CU(cudaMemcpy(d->blob, h.data(), total, cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
+    unsigned char* b = (unsigned char*)d->blob;
+    cusat::DevCode& c = d->code;
+    c.N = p.N;
+    c.K = p.K;
+    c.R = p.R;
+    c.q = p.q;
+    c.n_steps = p.n_steps;
+    c.cmax = p.cmax;
+    c.fast_lim = p.fast_lim;
+    c.msg_row = p.msg_row;
+    c.circ = (const uint32_t*)(b + o_circ);
+    c.cnt = (const uint8_t*)(b + o_cnt);
+    c.sched = (const int16_t*)(b + o_sched);
+    c.step_conf = (const uint8_t*)(b + o_conf);
+    return CUSAT_OK;
+}
+
+// Decoder engine shared by the plain decoder and the fused chain.
+struct Engine {
+    const cusat::CodePlan* plan = nullptr;
+    DevPlan dp;
+    int max_trials = 0, max_batch = 0, device = 0;
+    const void* fn = nullptr;
+    int threads = 0, grid_max = 0;
+    cusat::DecodeArgs proto{};
+    uint4* msg = nullptr;
+    unsigned int* queue = nullptr;
+
+    int init(const cusat::CodePlan* p, int trials, int batch, bool fused, int n_points)
+    {
+        plan = p;
+        max_trials = trials;
+        max_batch = batch;
+        int rc = require_device(&device);
+        if (rc)
+            return rc;
+        rc = upload_plan(*p, &dp);
+        if (rc)
+            return rc;
+        fn = cusat::select_decoder_kernel(p->cmax, p->lanes, fused);
+        if (!fn)
+            return fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel for this check degree");
+        threads = cusat::decoder_threads(p->lanes);
+        memset(&proto, 0, sizeof(proto));
+        proto.code = dp.code;
+        proto.max_trials = max_trials;
+        cusat::decoder_smem_layout(&proto, p->cmax, n_points);
+        int optin = 0, sms = 0;
+        CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
+        if (proto.sm_total > optin)
+            return fail(CUSAT_ERR_UNSUPPORTED, "frame state does not fit in shared memory");
+        CU(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, proto.sm_total),
+           "cudaFuncSetAttribute");
+        int per_sm = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, proto.sm_total),
+           "occupancy");
+        if (per_sm < 1)
+            return fail(CUSAT_ERR_UNSUPPORTED, "decoder kernel cannot be resident");
+        grid_max = per_sm * sms;
+        const size_t msg_bytes = (size_t)grid_max * p->R * p->msg_row;
+        CU(cudaMalloc(&msg, msg_bytes), "cudaMalloc(messages)");
+        CU(cudaMalloc(&queue, 256), "cudaMalloc(queue)");
+        proto.msg = msg;
+        proto.queue = queue;
+        return CUSAT_OK;
+    }
+
+    int launch(cusat::DecodeArgs a, int batch, cudaStream_t stream)
+    {
+        a.n_frames = batch;
+        const int grid = batch < grid_max ? batch : grid_max;
+        CU(cudaMemsetAsync(queue, 0, sizeof(unsigned int), stream), "cudaMemsetAsync(queue)");
+        const int rc = cusat::launch_decoder(fn, a, grid, threads, stream);
+        if (rc != 0)
+            return cuda_fail((cudaError_t)rc, "decoder launch");
+        return CUSAT_OK;
+    }
+
+    void release()
+    {
+        if (dp.blob)
+            cudaFree(dp.blob);
+        if (msg)
+            cudaFree(msg);
+        if (queue)
+            cudaFree(queue);
+        dp.blob = nullptr;
+        msg = nullptr;
+        queue = nullptr;
+    }
+};
+
+struct DevBch {
+    cusat::BchTables t;
+    void* blob = nullptr;
+    cusat::BchDev d{};
+
+    int init(const uint64_t* gen, int p, unsigned n_bytes)
+    {
+        std::string err;
+        if (!cusat::build_bch_tables(gen, p, n_bytes, &t, &err))
+            return fail(CUSAT_ERR_ARG, err);
+        const size_t nl = t.lut.size() * 8, nt = t.tree.size() * 8;
+        CU(cudaMalloc(&blob, nl + nt), "cudaMalloc(bch)");
+        CU(cudaMemcpy(blob, t.lut.data(), nl, cudaMemcpyHostToDevice), "cudaMemcpy(bch)");
+        CU(cudaMemcpy((char*)blob + nl, t.tree.data(), nt, cudaMemcpyHostToDevice), "cudaMemcpy(bch)");
+        d.p = t.p;
+        d.words = t.words;
+        d.n_bytes = t.n_bytes;
+        d.chunk = t.chunk;
+        d.lead = t.lead;
+        d.lut = (const uint64_t*)blob;
+        d.tree = (const uint64_t*)((char*)blob + nl);
+        return CUSAT_OK;
+    }
+    void release()
+    {
+        if (blob)
+            cudaFree(blob);
+        blob = nullptr;
+    }
+};
+
+struct DevDemapObj {
+    cusat::ModcodDemap m;
+    float2* pts = nullptr;
+    cusat::DevDemap d{};
+
+    int init(int mod, int rate, int fs)
+    {
+        std::string err;
+        if (!cusat::build_modcod_demap(mod, rate, fs, &m, &err))
+            return fail(CUSAT_ERR_UNSUPPORTED, err);
+        CU(cudaMalloc(&pts, m.pts.size() * 4), "cudaMalloc(points)");
+        CU(cudaMemcpy(pts, m.pts.data(), m.pts.size() * 4, cudaMemcpyHostToDevice), "cudaMemcpy(points)");
+        d.kind = m.kind;
+        d.n_mod = m.n_mod;
+        d.n_points = m.n_points;
+        d.xfec = m.xfec;
+        d.interleaved_len = m.interleaved_len;
+        d.fec_len = m.fec_len;
+        for (int b = 0; b < 8; b++)
+            d.col[b] = m.col[b];
+        d.points = pts;
+        return CUSAT_OK;
+    }
+    void release()
+    {
+        if (pts)
+            cudaFree(pts);
+        pts = nullptr;
+    }
+};
+
+}  // namespace
+
+struct cusat_ldpc_decoder {
+    Engine eng;
+    int16_t* soft_dev = nullptr;
+    uint8_t* hard_pinned = nullptr;
+    int32_t* trials_pinned = nullptr;
+};
+
+struct cusat_demapper {
+    DevDemapObj dm;
+    int max_batch = 0;
+    float* sym_dev = nullptr;
+    int16_t* soft_dev = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+struct cusat_bch_checker {
+    DevBch bch;
+};
+
+struct cusat_rx_fec {
+    Engine eng;
+    DevDemapObj dm;
+    DevBch bch;
+};
+
+extern "C" {
+
+const char* cusat_last_error(void) { return g_last_error.c_str(); }
+
+// --------------------------------------------------------------------------
+// LDPC decoder
+// --------------------------------------------------------------------------
+
+int cusat_ldpc_decoder_create(int framesize, int rate, int max_trials, int max_batch,
+                              cusat_ldpc_decoder** out)
+{
+    if (!out || max_trials < 0 || max_trials > 1000 || max_batch <= 0)
+        return fail(CUSAT_ERR_ARG, "invalid decoder arguments");
+    *out = nullptr;
+    std::string err;
+    const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
+    if (!p)
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    cusat_ldpc_decoder* d = new cusat_ldpc_decoder();
+    int rc = d->eng.init(p, max_trials, max_batch, false, 0);
+    if (rc == CUSAT_OK) {
+        cudaError_t e = cudaMalloc(&d->soft_dev, (size_t)max_batch * p->N * 2);
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&d->hard_pinned, (size_t)max_batch * (p->K / 8));
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&d->trials_pinned, (size_t)max_batch * 4);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "decoder buffers");
+    }
+    if (rc != CUSAT_OK) {
+        cusat_ldpc_decoder_destroy(d);
+        return rc;
+    }
+    *out = d;
+    return CUSAT_OK;
+}
+
+void cusat_ldpc_decoder_destroy(cusat_ldpc_decoder* d)
+{
+    if (!d)
+        return;
+    d->eng.release();
+    if (d->soft_dev)
+        cudaFree(d->soft_dev);
+    if (d->hard_pinned)
+        cudaFreeHost(d->hard_pinned);
+    if (d->trials_pinned)
+        cudaFreeHost(d->trials_pinned);
+    delete d;
+}
+
+int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* d, int32_t* out)
+{
+    if (!d || !out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    const cusat::CodePlan* p = d->eng.plan;
+    out[0] = p->N;
+    out[1] = p->K;
+    out[2] = p->K / 8;
+    out[3] = p->q;
+    out[4] = p->n_steps;
+    out[5] = d->eng.max_trials;
+    out[6] = d->eng.max_batch;
+    out[7] = p->lanes;
+    return CUSAT_OK;
+}
+
+int cusat_ldpc_decode_launch(cusat_ldpc_decoder* d, const int16_t* soft_dev, int batch, void* stream,
+                             uint8_t* hard_out, int32_t* trials_out)
+{
+    if (!d || !soft_dev)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    if (batch <= 0 || batch > d->eng.max_batch)
+        return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
+    cusat::DecodeArgs a = d->eng.proto;
+    a.llr = soft_dev;
+    a.hard = hard_out ? hard_out : d->hard_pinned;
+    a.trials = trials_out ? trials_out : d->trials_pinned;
+    return d->eng.launch(a, batch, (cudaStream_t)stream);
+}
+
+int cusat_ldpc_decode_batch(cusat_ldpc_decoder* d, const int16_t* soft_host, uint8_t* hard_host,
+                            int32_t* trials_host, int batch, void* stream)
+{
+    if (!d || !soft_host || !hard_host || !trials_host)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    if (batch <= 0 || batch > d->eng.max_batch)
+        return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
+    cudaStream_t s = (cudaStream_t)stream;
+    const cusat::CodePlan* p = d->eng.plan;
+    CU(cudaMemcpyAsync(d->soft_dev, soft_host, (size_t)batch * p->N * 2, cudaMemcpyHostToDevice, s),
+       "cudaMemcpyAsync(llr)");
+    int rc = cusat_ldpc_decode_launch(d, d->soft_dev, batch, stream, nullptr, nullptr);
+    if (rc)
+        return rc;
+    CU(cudaStreamSynchronize(s), "decode");
+    memcpy(hard_host, d->hard_pinned, (size_t)batch * (p->K / 8));
+    memcpy(trials_host, d->trials_pinned, (size_t)batch * 4);
+    return CUSAT_OK;
+}
+
+int cusat_ldpc_decode_batch_d2h(cusat_ldpc_decoder* d, const int16_t* soft_dev, uint8_t* hard_host,
+                                int32_t* trials_host, int batch, void* stream)
+{
+    if (!d || !hard_host || !trials_host)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    int rc = cusat_ldpc_decode_launch(d, soft_dev, batch, stream, nullptr, nullptr);
+    if (rc)
+        return rc;
+    CU(cudaStreamSynchronize((cudaStream_t)stream), "decode");
+    const cusat::CodePlan* p = d->eng.plan;
+    memcpy(hard_host, d->hard_pinned, (size_t)batch * (p->K / 8));
+    memcpy(trials_host, d->trials_pinned, (size_t)batch * 4);
+    return CUSAT_OK;
+}
+
+int cusat_ldpc_decoder_results(const cusat_ldpc_decoder* d, uint8_t* hard_host, int32_t* trials_host,
+                               int batch)
+{
+    if (!d || batch <= 0 || batch > d->eng.max_batch)
+        return fail(CUSAT_ERR_ARG, "invalid arguments");
+    const cusat::CodePlan* p = d->eng.plan;
+    if (hard_host)
+        memcpy(hard_host, d->hard_pinned, (size_t)batch * (p->K / 8));
+    if (trials_host)
+        memcpy(trials_host, d->trials_pinned, (size_t)batch * 4);
+    return CUSAT_OK;
+}
+
+// --------------------------------------------------------------------------
+// Demapper
+// --------------------------------------------------------------------------
+
+int cusat_demapper_create(int modulation, int rate, int framesize, int max_batch, cusat_demapper** out)
+{
+    if (!out || max_batch <= 0)
+        return fail(CUSAT_ERR_ARG, "invalid demapper arguments");
+    *out = nullptr;
+    int dev;
+    int rc = require_device(&dev);
+    if (rc)
+        return rc;
+    cusat_demapper* d = new cusat_demapper();
+    d->max_batch = max_batch;
+    rc = d->dm.init(modulation, rate, framesize);
+    if (rc == CUSAT_OK) {
+        cudaError_t e = cudaMalloc(&d->sym_dev, (size_t)max_batch * d->dm.m.xfec * 8);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&d->soft_dev, (size_t)max_batch * d->dm.m.fec_len * 2);
+        if (e == cudaSuccess)
+            e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "demapper buffers");
+    }
+    if (rc != CUSAT_OK) {
+        cusat_demapper_destroy(d);
+        return rc;
+    }
+    *out = d;
+    return CUSAT_OK;
+}
+
+void cusat_demapper_destroy(cusat_demapper* d)
+{
+    if (!d)
+        return;
+    d->dm.release();
+    if (d->sym_dev)
+        cudaFree(d->sym_dev);
+    if (d->soft_dev)
+        cudaFree(d->soft_dev);
+    if (d->stream)
+        cudaStreamDestroy(d->stream);
+    delete d;
+}
+
+int cusat_demapper_info(const cusat_demapper* d, int32_t* out)
+{
+    if (!d || !out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    out[0] = d->dm.m.fec_len;
+    out[1] = d->dm.m.xfec;
+    out[2] = d->dm.m.n_mod;
+    out[3] = d->dm.m.interleaved_len;
+    return CUSAT_OK;
+}
+
+float cusat_demapper_capped_llr_gain(const cusat_demapper* d, float llr_gain)
+{
+    return d ? cusat::capped_llr_gain(d->dm.m, llr_gain) : llr_gain;
+}
+
+int16_t* cusat_demapper_soft_out_dev(const cusat_demapper* d) { return d ? d->soft_dev : nullptr; }
+
+int cusat_demap_launch(cusat_demapper* d, const float* sym_dev, int batch, float noise_var, float llr_gain,
+                       int16_t* soft_out_dev, void* stream)
+{
+    if (!d || !sym_dev)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    if (batch <= 0 || batch > d->max_batch)
+        return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
+    const int rc = cusat::launch_demap(d->dm.d, sym_dev, batch, noise_var, llr_gain,
+                                       soft_out_dev ? soft_out_dev : d->soft_dev, (cudaStream_t)stream);
+    if (rc)
+        return cuda_fail((cudaError_t)rc, "demap launch");
+    return CUSAT_OK;
+}
+
+int cusat_demap_batch_async(cusat_demapper* d, const float* sym_host, int batch, float noise_var,
+                            float llr_gain, void* stream)
+{
+    if (!d || !sym_host)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    if (batch <= 0 || batch > d->max_batch)
+        return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
+    llr_gain = cusat::capped_llr_gain(d->dm.m, llr_gain);
+    CU(cudaMemcpyAsync(d->sym_dev, sym_host, (size_t)batch * d->dm.m.xfec * 8, cudaMemcpyHostToDevice,
+                       (cudaStream_t)stream),
+       "cudaMemcpyAsync(symbols)");
+    return cusat_demap_launch(d, d->sym_dev, batch, noise_var, llr_gain, nullptr, stream);
+}
+
+int cusat_demap_batch(cusat_demapper* d, const float* sym_host, int batch, float noise_var, float llr_gain)
+{
+    if (!d)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    const int rc = cusat_demap_batch_async(d, sym_host, batch, noise_var, llr_gain, d->stream);
+    if (rc)
+        return rc;
+    CU(cudaStreamSynchronize(d->stream), "demap");
+    return CUSAT_OK;
+}
+
+// --------------------------------------------------------------------------
+// BCH check
+// --------------------------------------------------------------------------
+
+int cusat_bch_checker_create(const uint64_t* flat_lut, const uint64_t* gen_poly, int gen_degree,
+                             unsigned int n_bytes, cusat_bch_checker** out)
+{
+    if (!out || !flat_lut || !gen_poly)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (gen_degree < 8 || gen_degree > 248 || (gen_degree & 7) || n_bytes <= (unsigned)(gen_degree / 8))
+        return fail(CUSAT_ERR_ARG, "invalid BCH checker geometry");
+    // the LUT must be the encoder table of this generator
+    uint64_t lut[256 * 4];
+    cusat::bch_encoder_lut(gen_poly, gen_degree, lut);
+    for (int b = 0; b < 256; b++)
+        for (int w = 0; w < (gen_degree + 63) / 64; w++)
+            if (lut[b * 4 + w] != flat_lut[b * 4 + w])
+                return fail(CUSAT_ERR_ARG, "BCH LUT does not match the generator");
+    int dev;
+    int rc = require_device(&dev);
+    if (rc)
+        return rc;
+    cusat_bch_checker* c = new cusat_bch_checker();
+    rc = c->bch.init(gen_poly, gen_degree, n_bytes);
+    if (rc) {
+        cusat_bch_checker_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return CUSAT_OK;
+}
+
+int cusat_bch_checker_create_for_code(int framesize, int rate, cusat_bch_checker** out)
+{
+    if (!out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    std::string err;
+    const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
+    if (!p)
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    uint64_t lut[256 * 4];
+    cusat::bch_encoder_lut(p->gen, p->p, lut);
+    return cusat_bch_checker_create(lut, p->gen, p->p, (unsigned)(p->n_bch / 8), out);
+}
+
+void cusat_bch_checker_destroy(cusat_bch_checker* c)
+{
+    if (!c)
+        return;
+    c->bch.release();
+    delete c;
+}
+
+unsigned int cusat_bch_checker_n_bytes(const cusat_bch_checker* c) { return c ? c->bch.t.n_bytes : 0; }
+
+int cusat_bch_check_launch(cusat_bch_checker* c, const uint8_t* codewords_dev, int32_t* valid_out,
+                           uint8_t* rem_out, int batch, void* stream)
+{
+    if (!c)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    if (batch < 0)
+        return fail(CUSAT_ERR_ARG, "negative BCH batch");
+    if (batch == 0)
+        return CUSAT_OK;
+    if (!codewords_dev || (!valid_out && !rem_out))
+        return fail(CUSAT_ERR_ARG, "null BCH checker buffer");
+    const int rc = cusat::launch_bch_check(c->bch.d, codewords_dev, valid_out, rem_out, batch,
+                                           (cudaStream_t)stream);
+    if (rc)
+        return cuda_fail((cudaError_t)rc, "BCH launch");
+    return CUSAT_OK;
+}
+
+// --------------------------------------------------------------------------
+// Fused receive chain
+// --------------------------------------------------------------------------
+
+int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials, int max_batch,
+                        cusat_rx_fec** out)
+{
+    if (!out || max_trials < 0 || max_trials > 1000 || max_batch <= 0)
+        return fail(CUSAT_ERR_ARG, "invalid arguments");
+    *out = nullptr;
+    std::string err;
+    const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
+    if (!p)
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    cusat_rx_fec* r = new cusat_rx_fec();
+    int rc = r->dm.init(modulation, rate, framesize);
+    if (rc == CUSAT_OK)
+        rc = r->eng.init(p, max_trials, max_batch, true, r->dm.m.kind == 2 ? r->dm.m.n_points : 0);
+    if (rc == CUSAT_OK)
+        rc = r->bch.init(p->gen, p->p, (unsigned)(p->n_bch / 8));
+    if (rc == CUSAT_OK) {
+        r->eng.proto.dm = r->dm.d;
+    }
+    if (rc != CUSAT_OK) {
+        cusat_rx_fec_destroy(r);
+        return rc;
+    }
+    *out = r;
+    return CUSAT_OK;
+}
+
+void cusat_rx_fec_destroy(cusat_rx_fec* r)
+{
+    if (!r)
+        return;
+    r->eng.release();
+    r->dm.release();
+    r->bch.release();
+    delete r;
+}
+
+int cusat_rx_fec_info(const cusat_rx_fec* r, int32_t* out)
+{
+    if (!r || !out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    const cusat::CodePlan* p = r->eng.plan;
+    out[0] = r->dm.m.xfec;
+    out[1] = p->N;
+    out[2] = p->K;
+    out[3] = p->K / 8;
+    out[4] = p->k_bch;
+    out[5] = r->dm.m.n_mod;
+    return CUSAT_OK;
+}
+
+float cusat_rx_fec_capped_llr_gain(const cusat_rx_fec* r, float llr_gain)
+{
+    return r ? cusat::capped_llr_gain(r->dm.m, llr_gain) : llr_gain;
+}
+
+int cusat_rx_fec_launch(cusat_rx_fec* r, const float* sym_dev, int batch, float noise_var, float llr_gain,
+                        uint8_t* hard_out, int32_t* trials_out, int32_t* bch_valid_out, void* stream)
+{
+    if (!r || !sym_dev || !hard_out || !trials_out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    if (batch <= 0 || batch > r->eng.max_batch)
+        return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
+    if (r->dm.m.interleaved_len != r->dm.m.xfec)
+        return fail(CUSAT_ERR_UNSUPPORTED, "padded XFECFRAME");
+    cusat::DecodeArgs a = r->eng.proto;
+    a.sym = sym_dev;
+    a.noise_var = noise_var;
+    a.llr_gain = cusat::capped_llr_gain(r->dm.m, llr_gain);
+    a.hard = hard_out;
+    a.trials = trials_out;
+    int rc = r->eng.launch(a, batch, (cudaStream_t)stream);
+    if (rc)
+        return rc;
+    if (bch_valid_out) {
+        const int e = cusat::launch_bch_check(r->bch.d, hard_out, bch_valid_out, nullptr, batch,
+                                              (cudaStream_t)stream);
+        if (e)
+            return cuda_fail((cudaError_t)e, "BCH launch");
+    }
+    return CUSAT_OK;
+}
+
+// --------------------------------------------------------------------------
+// Code description and traffic generation (host side, not on the receive path)
+// --------------------------------------------------------------------------
+
+int cusat_code_info(int framesize, int rate, int32_t* out)
+{
+    if (!out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    std::string err;
+    const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
+    if (!p)
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    out[0] = p->N;
+    out[1] = p->K;
+    out[2] = p->k_bch;
+    out[3] = p->n_bch;
+    out[4] = p->t;
+    out[5] = p->p;
+    out[6] = p->q;
+    out[7] = p->n_steps;
+    out[8] = p->lanes;
+    out[9] = p->cmax;
+    out[10] = p->links_total;
+    out[11] = p->cnt_max;
+    return CUSAT_OK;
+}
+
+int cusat_gen_encode(int framesize, int rate, const uint8_t* msg, uint8_t* cw, int batch)
+{
+    if (!msg || !cw || batch < 0)
+        return fail(CUSAT_ERR_ARG, "invalid arguments");
+    std::string err;
+    const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
+    if (!p)
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    std::vector<uint8_t> bch((size_t)p->n_bch / 8);
+    for (int f = 0; f < batch; f++) {
+        cusat::bch_encode_frames(*p, msg + (size_t)f * (p->k_bch / 8), bch.data(), 1);
+        cusat::ldpc_encode_frames(*p, bch.data(), cw + (size_t)f * (p->N / 8), 1);
+    }
+    return CUSAT_OK;
+}
+
+int cusat_gen_map(int modulation, int rate, int framesize, const uint8_t* cw, int batch, float* sym)
+{
+    if (!cw || !sym || batch < 0)
+        return fail(CUSAT_ERR_ARG, "invalid arguments");
+    cusat::ModcodDemap m;
+    std::string err;
+    if (!cusat::build_modcod_demap(modulation, rate, framesize, &m, &err))
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    cusat::map_frames(m, cw, batch, sym);
+    return CUSAT_OK;
+}
+
+int cusat_modcod_info(int modulation, int rate, int framesize, float* points, uint32_t* col, int32_t* out)
+{
+    cusat::ModcodDemap m;
+    std::string err;
+    if (!cusat::build_modcod_demap(modulation, rate, framesize, &m, &err))
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    if (points)
+        memcpy(points, m.pts.data(), m.pts.size() * 4);
+    if (col)
+        memcpy(col, m.col, sizeof(m.col));
+    if (out) {
+        out[0] = m.n_mod;
+        out[1] = m.n_points;
+        out[2] = m.fec_len;
+        out[3] = m.xfec;
+        out[4] = m.interleaved_len;
+        out[5] = m.kind;
+    }
+    return CUSAT_OK;
+}
+
+float cusat_modcod_capped_llr_gain(int modulation, int rate, int framesize, float llr_gain)
+{
+    cusat::ModcodDemap m;
+    std::string err;
+    if (!cusat::build_modcod_demap(modulation, rate, framesize, &m, &err))
+        return llr_gain;
+    return cusat::capped_llr_gain(m, llr_gain);
+}
+
+}  // extern "C"

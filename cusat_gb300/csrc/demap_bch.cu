@@ -1,0 +1,136 @@
+// Standalone soft demapper and BCH syndrome-check kernels.
+#include "fec_device.cuh"
+#include "kernels.h"
+
+namespace cusat {
+
+// One thread per symbol (grid.y = frame), points staged in shared memory.
+// Reference cuda/demapper_kernel.cu:31-184 (same arithmetic as the decoder's
+// fused prologue: demap_symbol).
+__global__ void __launch_bounds__(256) demap_kernel(DevDemap d, const float2* __restrict__ sym,
+                                                   int16_t* __restrict__ out, float noise_var,
+                                                   float llr_gain)
+{
+    __shared__ float2 pts[256];
+    if (d.kind == 2)
+        for (int k = threadIdx.x; k < d.n_points; k += blockDim.x)
+            pts[k] = d.points[k];
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.y;
+    if (j >= d.interleaved_len)
+        return;
+    const float2 s = __ldcs(sym + (size_t)f * d.xfec + j);
+    int pos[8];
+    int16_t l[8];
+    const int nb = demap_symbol(d, pts, s.x, s.y, j, noise_var, llr_gain, pos, l);
+    int16_t* o = out + (size_t)f * d.fec_len;
+#pragma unroll
+    for (int b = 0; b < 8; b++)
+        if (b < nb && pos[b] < d.fec_len)
+            o[pos[b]] = l[b];
+}
+
+int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
+                 int16_t* out, cudaStream_t stream)
+{
+    dim3 grid((d.interleaved_len + 255) / 256, batch);
+    demap_kernel<<<grid, 256, 0, stream>>>(d, reinterpret_cast<const float2*>(sym), out, noise_var,
+                                           llr_gain);
+    return (int)cudaGetLastError();
+}
+
+// BCH check: one warp per frame.  Lane l runs the byte-LUT LFSR
+// r <- (r x^8 + b x^p) mod g over bytes [l chunk, (l+1) chunk) of the frame
+// front-padded with zero bytes to 32 chunks (leading zeros leave the
+// remainder unchanged).  The 32 lane remainders are then combined in five
+// shuffle levels: at level k the earlier block A and the later block B of
+// each pair give A x^(8 chunk 2^k) + B mod g, the multiplication being a
+// XOR of per-byte tables.  The result is c(x) x^p mod g(x), which is zero iff
+// c is a codeword.  Reference cuda/bch_common.cuh:91-158.
+template <int W>
+__global__ void __launch_bounds__(128) bch_check_kernel(BchDev t, const uint8_t* __restrict__ cw,
+                                                        int32_t* __restrict__ valid,
+                                                        uint8_t* __restrict__ rem, int batch)
+{
+    __shared__ uint64_t lut[256 * W];
+    for (int k = threadIdx.x; k < 256 * W; k += blockDim.x)
+        lut[k] = t.lut[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (f >= batch)
+        return;
+    const int p = t.p;
+    const uint64_t top_mask = (p % 64) ? ((1ull << (p % 64)) - 1) : ~0ull;
+    const uint8_t* src = cw + (size_t)f * t.n_bytes;
+    uint64_t r[W];
+#pragma unroll
+    for (int w = 0; w < W; w++)
+        r[w] = 0;
+    const int v0 = lane * t.chunk, v1 = v0 + t.chunk;
+    for (int v = max(v0, (int)t.lead); v < v1; v++) {
+        const unsigned b = src[v - t.lead];
+        const int lo = p - 8;
+        const unsigned idx = b ^ (unsigned)((r[lo >> 6] >> (lo & 63)) & 255);
+#pragma unroll
+        for (int w = W - 1; w >= 0; w--)
+            r[w] = (r[w] << 8) | (w ? r[w - 1] >> 56 : 0);
+        r[W - 1] &= top_mask;
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            r[w] ^= lut[idx * W + w];
+    }
+    const int nb = p / 8;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        uint64_t o[W], a[W], acc[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            o[w] = __shfl_xor_sync(0xffffffffu, r[w], 1 << k);
+            a[w] = (lane & (1 << k)) ? o[w] : r[w];
+            acc[w] = (lane & (1 << k)) ? r[w] : o[w];
+        }
+        const uint64_t* tk = t.tree + (size_t)k * nb * 256 * W;
+        for (int jb = 0; jb < nb; jb++) {
+            const unsigned byte = (unsigned)((a[jb >> 3] >> ((jb & 7) * 8)) & 255);
+            const uint64_t* e = tk + ((size_t)jb * 256 + byte) * W;
+#pragma unroll
+            for (int w = 0; w < W; w++)
+                acc[w] ^= __ldg(e + w);
+        }
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            r[w] = acc[w];
+    }
+    if (lane == 0) {
+        uint64_t any = 0;
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            any |= r[w];
+        if (valid)
+            valid[f] = any == 0;
+        if (rem)
+            for (int jb = 0; jb < nb; jb++) {
+                const int lo = p - 8 * (jb + 1);
+                rem[(size_t)f * nb + jb] = (uint8_t)(r[lo >> 6] >> (lo & 63));
+            }
+    }
+}
+
+int launch_bch_check(const BchDev& t, const uint8_t* cw, int32_t* valid, uint8_t* rem, int batch,
+                     cudaStream_t stream)
+{
+    const int blocks = (batch + 3) / 4;
+    if (t.words == 1)
+        bch_check_kernel<1><<<blocks, 128, 0, stream>>>(t, cw, valid, rem, batch);
+    else if (t.words == 2)
+        bch_check_kernel<2><<<blocks, 128, 0, stream>>>(t, cw, valid, rem, batch);
+    else if (t.words == 3)
+        bch_check_kernel<3><<<blocks, 128, 0, stream>>>(t, cw, valid, rem, batch);
+    else
+        bch_check_kernel<4><<<blocks, 128, 0, stream>>>(t, cw, valid, rem, batch);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace cusat

@@ -1,0 +1,40 @@
+// Launchers of the FEC kernels (host-callable, defined in the .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fec_device.cuh"
+
+namespace cusat {
+
+struct DecodeArgs;
+
+// BCH check tables in device memory (host.h BchTables layout).
+struct BchDev {
+    int p, words;
+    unsigned n_bytes, chunk, lead;
+    const uint64_t* lut;   // [256 * words]
+    const uint64_t* tree;  // [5][p/8][256][words]
+};
+
+// Shared-memory layout and limits of one decoder kernel instantiation.
+struct DecoderKernelInfo {
+    const void* fn;
+    int threads;
+    int blocks_per_sm;
+};
+
+// Fills the shared-memory carve-up of a and returns the kernel to launch
+// (nullptr if the (cmax, lanes) pair has no instantiation).
+const void* select_decoder_kernel(int cmax, int lanes, bool fused);
+void decoder_smem_layout(DecodeArgs* a, int cmax, int n_points);
+int decoder_threads(int lanes);
+int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
+
+int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
+                 int16_t* out, cudaStream_t stream);
+int launch_bch_check(const BchDev& t, const uint8_t* cw, int32_t* valid, uint8_t* rem, int batch,
+                     cudaStream_t stream);
+
+}  // namespace cusat

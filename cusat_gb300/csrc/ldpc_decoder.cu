@@ -1,0 +1,65 @@
+// Instantiations and launch helpers of the layered decoder kernel.
+#include "kernels.h"
+#include "ldpc_kernel.cuh"
+
+namespace cusat {
+
+namespace {
+
+template <int CMAX>
+const void* pick(int lanes, bool fused)
+{
+    if (lanes == 2)
+        return fused ? (const void*)ldpc_layered_kernel<CMAX, 2, true>
+                     : (const void*)ldpc_layered_kernel<CMAX, 2, false>;
+    return fused ? (const void*)ldpc_layered_kernel<CMAX, 1, true>
+                 : (const void*)ldpc_layered_kernel<CMAX, 1, false>;
+}
+
+int align16(int x) { return (x + 15) & ~15; }
+
+}  // namespace
+
+const void* select_decoder_kernel(int cmax, int lanes, bool fused)
+{
+    switch (cmax) {
+    case 3: return pick<3>(lanes, fused);
+    case 5: return pick<5>(lanes, fused);
+    case 9: return pick<9>(lanes, fused);
+    case 14: return pick<14>(lanes, fused);
+    case 20: return pick<20>(lanes, fused);
+    case 28: return pick<28>(lanes, fused);
+    default: return nullptr;
+    }
+}
+
+int decoder_threads(int lanes) { return lanes * kLaneThreads; }
+
+void decoder_smem_layout(DecodeArgs* a, int cmax, int n_points)
+{
+    const DevCode& c = a->code;
+    int off = align16(c.N * 2);
+    a->sm_stage = off;
+    off = align16(off + kMaxStage * kM * 2);
+    a->sm_circ = off;
+    off = align16(off + c.q * cmax * 4);
+    a->sm_sched = off;
+    off = align16(off + c.n_steps * 4);
+    a->sm_cnt = off;
+    off = align16(off + c.q);
+    a->sm_conf = off;
+    off = align16(off + c.n_steps);
+    a->sm_pts = off;
+    off = align16(off + n_points * 8);
+    a->sm_misc = off;
+    off = align16(off + 16);
+    a->sm_total = off;
+}
+
+int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream)
+{
+    void* args[] = {const_cast<DecodeArgs*>(&a)};
+    return (int)cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, (size_t)a.sm_total, stream);
+}
+
+}  // namespace cusat

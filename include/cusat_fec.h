@@ -1,0 +1,202 @@
+/*
+ * cusat_fec.h -- C ABI of the GB300 receive-side FEC path.
+ *
+ * Soft demapping with deinterleave, layered offset min-sum LDPC decoding of
+ * the DVB-S2/S2X codes on int16 LLRs with a syndrome early exit, and the BCH
+ * syndrome check, as hand-written sm_103a CUDA kernels behind plain C entry
+ * points (pointers, sizes, ints; no CUDA or C++ types).  `stream` arguments
+ * are cudaStream_t values passed as void*; NULL is the legacy default stream.
+ * Device pointers are device (or mapped pinned) memory; "host" pointers are
+ * ordinary host memory.
+ *
+ * Enumerations (frame size, code rate, modulation) use the numeric values of
+ * the reference's lib/cusat_dsp/include/cusat_dsp/modcod_types.h:14-95, so a
+ * caller of the reference passes its own enum values unchanged.
+ *
+ * Every entry point returns CUSAT_OK (0) or a negative CUSAT_ERR_* code;
+ * cusat_last_error() returns a one-line description of the last failure on
+ * the calling thread.  Objects are not thread-safe (like the reference's
+ * classes); distinct objects may be used from distinct threads.
+ *
+ * Results follow the reference conventions: trials[f] = max_trials -
+ * iterations used when the syndrome is satisfied, -1 after max_trials
+ * iterations without convergence; hard decisions are the k_ldpc information
+ * bits, packed MSB-first (k_ldpc/8 bytes per frame); bch_valid[f] = 1 when
+ * the hard decisions are a BCH codeword.
+ */
+#ifndef CUSAT_FEC_H
+#define CUSAT_FEC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUSAT_OK 0
+#define CUSAT_ERR_ARG (-1)          /* invalid argument (batch, pointer, size) */
+#define CUSAT_ERR_UNSUPPORTED (-2)  /* frame size / rate / modulation not supported */
+#define CUSAT_ERR_CUDA (-3)         /* CUDA runtime error (message in cusat_last_error) */
+#define CUSAT_ERR_NO_DEVICE (-4)    /* no CUDA device */
+
+const char* cusat_last_error(void);
+
+/* ---------------------------------------------------------------------- */
+/* LDPC decoder                                                            */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_ldpc_decoder cusat_ldpc_decoder;
+
+/* Replaces cusat_dsp::cuda::ldpc_decode_cuda::ldpc_decode_cuda
+ * (reference lib/cusat_dsp/cuda/ldpc_decode_kernel.cuh:22-35, .cu:990-1181)
+ * and cusat_dsp::ldpc_decode::ldpc_decode (lib/cusat_dsp/ldpc_decode.h:22-33):
+ * builds the code's decoding plan on the current device and reserves
+ * buffers for up to max_batch frames. */
+int cusat_ldpc_decoder_create(int framesize, int rate, int max_trials, int max_batch,
+                              cusat_ldpc_decoder** out);
+void cusat_ldpc_decoder_destroy(cusat_ldpc_decoder* dec);
+
+/* out[0..7] = n_bits, k_bits, k_bytes, q, n_steps, max_trials, max_batch,
+ * lanes (2 = paired-layer schedule) */
+int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* dec, int32_t* out);
+
+/* Replaces ldpc_decode_cuda::decode_launch_async (ldpc_decode_kernel.cuh:51-64,
+ * .cu:1324-1336): decodes `batch` frames of n_bits int16 LLRs read from
+ * device memory, asynchronously on `stream`.  hard_out (batch*k_bytes) and
+ * trials_out (batch) are device or mapped pinned pointers; NULL selects the
+ * decoder's internal pinned buffers (read them with _results after a sync). */
+int cusat_ldpc_decode_launch(cusat_ldpc_decoder* dec, const int16_t* soft_dev, int batch,
+                             void* stream, uint8_t* hard_out, int32_t* trials_out);
+
+/* Replaces ldpc_decode_cuda::decode_batch (ldpc_decode_kernel.cuh:37-49,
+ * .cu:1287-1305) and ldpc_decode::decode_batch_cuda (ldpc_decode.h:35-44):
+ * host LLRs in, host results out, synchronous on `stream`. */
+int cusat_ldpc_decode_batch(cusat_ldpc_decoder* dec, const int16_t* soft_host, uint8_t* hard_host,
+                            int32_t* trials_host, int batch, void* stream);
+
+/* Replaces ldpc_decode_cuda::decode_batch_d2h (ldpc_decode_kernel.cuh:44-49,
+ * .cu:1307-1322) and ldpc_decode::decode_batch_cuda_d2h (ldpc_decode.h:46-53):
+ * device LLRs in, host results out, synchronous on `stream`. */
+int cusat_ldpc_decode_batch_d2h(cusat_ldpc_decoder* dec, const int16_t* soft_dev,
+                                uint8_t* hard_host, int32_t* trials_host, int batch, void* stream);
+
+/* Copies the internal result buffers of the last launch that used them. */
+int cusat_ldpc_decoder_results(const cusat_ldpc_decoder* dec, uint8_t* hard_host,
+                               int32_t* trials_host, int batch);
+
+/* ---------------------------------------------------------------------- */
+/* Soft demapper + deinterleaver                                           */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_demapper cusat_demapper;
+
+/* Replaces cusat_dsp::cuda::demapper_cuda::demapper_cuda
+ * (lib/cusat_dsp/cuda/demapper_kernel.cuh:23-38, .cu:188-281). */
+int cusat_demapper_create(int modulation, int rate, int framesize, int max_batch,
+                          cusat_demapper** out);
+void cusat_demapper_destroy(cusat_demapper* dm);
+
+/* out[0..3] = fecframe_len, xfecframe_len, n_mod, interleaved_len */
+int cusat_demapper_info(const cusat_demapper* dm, int32_t* out);
+
+/* Replaces demapper_cuda::capped_llr_gain (demapper_kernel.cuh:68-70,
+ * .cu:283-291). */
+float cusat_demapper_capped_llr_gain(const cusat_demapper* dm, float llr_gain);
+
+/* Device pointer of the internal LLR buffer [max_batch * fecframe_len]
+ * (replaces demapper_cuda::soft_out_dev, demapper_kernel.cuh:72-73). */
+int16_t* cusat_demapper_soft_out_dev(const cusat_demapper* dm);
+
+/* Demaps symbols already on the device (batch * xfecframe_len complex
+ * float pairs) into soft_out_dev (NULL = internal buffer), async. */
+int cusat_demap_launch(cusat_demapper* dm, const float* sym_dev, int batch, float noise_var,
+                       float llr_gain, int16_t* soft_out_dev, void* stream);
+
+/* Replaces demapper_cuda::demap_batch_async (demapper_kernel.cuh:53-66,
+ * .cu:335-362): copies host symbols to the device and demaps into the
+ * internal buffer, asynchronously on `stream` (llr_gain is capped first). */
+int cusat_demap_batch_async(cusat_demapper* dm, const float* sym_host, int batch,
+                            float noise_var, float llr_gain, void* stream);
+
+/* Replaces demapper_cuda::demap_batch (demapper_kernel.cuh:40-51,
+ * .cu:302-333): as _async, then synchronizes. */
+int cusat_demap_batch(cusat_demapper* dm, const float* sym_host, int batch, float noise_var,
+                      float llr_gain);
+
+/* ---------------------------------------------------------------------- */
+/* BCH syndrome check                                                      */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_bch_checker cusat_bch_checker;
+
+/* Replaces cusat_dsp::cuda::bch_check_cuda::bch_check_cuda
+ * (lib/cusat_dsp/cuda/bch_check_kernel.cuh:9-24, .cu:13-23): flat_lut is
+ * the reference's 256 x 4 uint64 encoder LUT (bch_code_t::encoder_lut),
+ * gen_poly the 4-word generator, n_bytes the codeword length in bytes. */
+int cusat_bch_checker_create(const uint64_t* flat_lut, const uint64_t* gen_poly, int gen_degree,
+                             unsigned int n_bytes, cusat_bch_checker** out);
+/* Same checker built from the standard code of (framesize, rate). */
+int cusat_bch_checker_create_for_code(int framesize, int rate, cusat_bch_checker** out);
+void cusat_bch_checker_destroy(cusat_bch_checker* bc);
+unsigned int cusat_bch_checker_n_bytes(const cusat_bch_checker* bc);
+
+/* Replaces bch_check_cuda::check_async (bch_check_kernel.cu:26-36):
+ * valid_out[f] = 1 iff codeword f (n_bytes, device) is a BCH codeword.
+ * rem_out (NULL or batch * degree/8 bytes) receives c(x) x^p mod g(x),
+ * coefficient of x^(p-1) first. */
+int cusat_bch_check_launch(cusat_bch_checker* bc, const uint8_t* codewords_dev,
+                           int32_t* valid_out, uint8_t* rem_out, int batch, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Fused receive chain for one MODCOD                                      */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_rx_fec cusat_rx_fec;
+
+/* One MODCOD's demap + deinterleave -> LDPC decode -> BCH check, fused in
+ * one decoder launch (the demap runs in the decoder's prologue, the
+ * LLRs never leave shared memory) followed by the BCH check.  Replaces the
+ * per-slot launch sequence of rx_fec_chain::launch_slot_gpu
+ * (lib/cusat_dsp/rx_fec_chain.cc:361-505). */
+int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials, int max_batch,
+                        cusat_rx_fec** out);
+void cusat_rx_fec_destroy(cusat_rx_fec* rx);
+/* out[0..5] = xfecframe_len, n_bits, k_bits, k_bytes, k_bch, n_mod */
+int cusat_rx_fec_info(const cusat_rx_fec* rx, int32_t* out);
+float cusat_rx_fec_capped_llr_gain(const cusat_rx_fec* rx, float llr_gain);
+/* Symbols on the device in, results to device or mapped pinned memory;
+ * llr_gain is capped like demap_batch does (demapper_kernel.cu:283-291). */
+int cusat_rx_fec_launch(cusat_rx_fec* rx, const float* sym_dev, int batch, float noise_var,
+                        float llr_gain, uint8_t* hard_out, int32_t* trials_out,
+                        int32_t* bch_valid_out, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Code description and traffic generation (host side; used to generate     */
+/* test and benchmark traffic, not part of the receive path)               */
+/* ---------------------------------------------------------------------- */
+
+/* out[0..11] = n_ldpc, k_ldpc, k_bch, n_bch, t, bch_degree, q, n_steps,
+ * lanes, kernel slot bucket, Tanner edges, largest circulants per layer.
+ * Reference get_fec_params (lib/cusat_dsp/fec/code_params.cc:102-108) and
+ * create_ldpc_table (lib/cusat_dsp/ldpc_table_factory.cc:97-102). */
+int cusat_code_info(int framesize, int rate, int32_t* out);
+/* BCH + LDPC encode: msg k_bch/8 bytes -> codeword n_ldpc/8 bytes per frame
+ * (reference bch_encode fec/bch_code.cc:124-144, IRA encoder
+ * ldpc_encode.cc:6-13). */
+int cusat_gen_encode(int framesize, int rate, const uint8_t* msg, uint8_t* cw, int batch);
+/* Interleave + map codewords to xfecframe_len symbols (re, im) per frame
+ * (reference mapper.cc:75-86, cuda/mapper_kernel.cu:22-51). */
+int cusat_gen_map(int modulation, int rate, int framesize, const uint8_t* cw, int batch, float* sym);
+/* Constellation points (2 * n_points floats, by label), interleaver column
+ * offsets (8) and out[0..5] = n_mod, n_points, fecframe_len, xfecframe_len,
+ * interleaved_len, demap kind (0 QPSK, 1 8PSK, 2 log-MAP).  Reference
+ * make_constellation (modulation/constellation.cc:461) and
+ * make_bit_interleaver (modulation/bit_interleaver.cc:76-96). */
+int cusat_modcod_info(int modulation, int rate, int framesize, float* points, uint32_t* col,
+                      int32_t* out);
+float cusat_modcod_capped_llr_gain(int modulation, int rate, int framesize, float llr_gain);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUSAT_FEC_H */

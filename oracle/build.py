@@ -1,0 +1,78 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+* ``oracle/_build/libfec_oracle.so`` -- the C restatement in fec_oracle.c.
+* ``oracle/_ref/libcusat_ref_host.so`` -- when the reference tree is present
+  (never on the GPU host), the reference's own host-side code for this path
+  (code parameters, BCH generator/encoder, bit interleaver, constellations,
+  table factory, message clamp) compiled unchanged from where it lies,
+  together with ``ref_shim.cc`` (this project's extern "C" accessors), so
+  that tests can compare the restatement with the reference itself.
+
+Usage: python3 oracle/build.py   (also run by __graft_entry__.build()).
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("CUSAT_REFERENCE_TREE", "/root/reference")
+REF_SOURCES = [
+    "lib/cusat_dsp/fec/code_params.cc",
+    "lib/cusat_dsp/fec/bch_code.cc",
+    "lib/cusat_dsp/modulation/bit_interleaver.cc",
+    "lib/cusat_dsp/modulation/constellation.cc",
+    "lib/cusat_dsp/ldpc_table_factory.cc",
+]
+
+
+def _newer(out, deps):
+    if not os.path.exists(out):
+        return False
+    t = os.path.getmtime(out)
+    return all(os.path.getmtime(d) <= t for d in deps)
+
+
+def build_oracle(verbose=False):
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libfec_oracle.so")
+    deps = [os.path.join(HERE, "fec_oracle.c"), os.path.join(HERE, "fec_oracle.h"),
+            os.path.join(HERE, "..", "cusat_gb300", "csrc", "cusat_data.h"),
+            os.path.join(HERE, "..", "cusat_gb300", "csrc", "gen", "code_tables.inc")]
+    if _newer(out, deps):
+        return out
+    cmd = ["gcc", "-std=c99", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           "-o", out + ".tmp", os.path.join(HERE, "fec_oracle.c"), "-lm"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build_ref(verbose=False):
+    """Compile the reference's host code; returns the path or None if absent."""
+    if not os.path.isdir(os.path.join(REF, "lib", "cusat_dsp")):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libcusat_ref_host.so")
+    srcs = [os.path.join(REF, s) for s in REF_SOURCES]
+    shim = os.path.join(HERE, "ref_shim.cc")
+    if _newer(out, srcs + [shim]):
+        return out
+    inc = ["-I" + os.path.join(REF, "lib", "cusat_dsp"),
+           "-I" + os.path.join(REF, "lib", "cusat_dsp", "include")]
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", *inc,
+           "-o", out + ".tmp", shim, *srcs]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle(verbose=True))
+    print(build_ref(verbose=True))
+    sys.exit(0)

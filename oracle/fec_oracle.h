@@ -1,0 +1,85 @@
+/*
+ * CPU oracle for the receive-side FEC path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's algorithms, used as the checker by
+ * tests/, by __graft_entry__.smoke() and as the timed CPU baseline of
+ * bench.py.  Nothing in the product (cusat_gb300/) links, loads or calls it.
+ *
+ * Decoder semantics (reference lib/cusat_dsp/cuda/ldpc_decode_kernel.cu):
+ *   - APP init with the -32768 -> -32767 clamp and the parity transpose
+ *     pty[M*i + j] = llr[K + q*j + i]                          (:635-684)
+ *   - syndrome before every iteration, trials = T - t on success, -1 after
+ *     T iterations                                          (:689-749, :943)
+ *   - layer update: x = qsat16(APP - old), offset min-sum finalp with
+ *     beta = 1, message = clamp8, info APP += msg - old (saturating),
+ *     parity APP = sat16(x + msg)                       (:242-275, :761-837)
+ *   - the reference leaves checks of one schedule step that share a variable
+ *     node to a data race (:793-802); the oracle resolves it as step-Jacobi:
+ *     every check of a step gathers from the APP state at the start of the
+ *     step and a shared variable node receives sat16(APP + sum of deltas).
+ * Parity pinned by: the message clamp/delta known answers of
+ * lib/qa_ldpc_message_update.cc:10-27, the BCH tests of lib/qa_bch_code.cc
+ * and apps/bench_bch_gpu.cc:52-104, the table manifest
+ * lib/cusat_dsp/ldpc_tables/checksums.txt, the noiseless round trips of
+ * lib/qa_ldpc_encode.cc:35-87 and, where the reference tree is present, the
+ * reference's own host code compiled into oracle/_ref.  The reference has no
+ * CPU decoder and no decoder golden vector, so iteration-level decoder
+ * behaviour on noisy input is pinned only through these round trips.
+ */
+#ifndef FEC_ORACLE_H
+#define FEC_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* out[0..9] = N, K, q, n_steps, k_bch, n_bch, t, bch_degree, links_total, cnl */
+int orc_code_info(int framesize, int rate, int32_t* out);
+
+/* Decodes B frames of N int16 LLRs. hard: B*K/8 bytes MSB-first;
+ * trials: T - iterations used, or -1. weights (may be NULL): per iteration t
+ * (0..T-1) and check degree d (0..31) an int16 pair {beta, alpha64} at
+ * weights[(t*32 + d)*2]; NULL = offset min-sum beta 1, no scaling. */
+int orc_ldpc_decode(int framesize, int rate, const int16_t* llr, int B, int max_trials,
+                    const int16_t* weights, uint8_t* hard, int32_t* trials, int nthreads);
+
+/* Syndrome of hard decisions from APP signs (test helper): 1 if every
+ * parity check of the int16 LLR vector (< 0 = bit 1) is satisfied. */
+int orc_syndrome_ok(int framesize, int rate, const int16_t* llr);
+
+/* IRA encode: info K/8 bytes -> codeword N/8 bytes (info then parity). */
+int orc_ldpc_encode(int framesize, int rate, const uint8_t* info, uint8_t* cw, int B);
+
+/* BCH generator (bit i of word i/64 = coeff of x^i), returns its degree. */
+int orc_bch_generator(int framesize, int rate, uint64_t gen[4]);
+/* Systematic BCH encode: k_bch/8 bytes -> n_bch/8 bytes. */
+int orc_bch_encode(int framesize, int rate, const uint8_t* msg, uint8_t* cw, int B);
+/* Bit-serial remainder of n_bch/8-byte words mod g: rem (p/8 bytes, the
+ * coefficient of x^(p-1) first) and valid = (rem == 0). */
+int orc_bch_check(int framesize, int rate, const uint8_t* cw, uint8_t* rem, int32_t* valid,
+                  int B);
+
+/* Soft demap + deinterleave (reference cuda/demapper_kernel.cu:31-184).
+ * kind 0 = QPSK formula, 1 = 8PSK formula, 2 = log-MAP over the points. */
+int orc_demap(const float* sym, int B, int xfec, int interleaved_len, int fec_len, int n_mod,
+              int kind, const float* pts_re, const float* pts_im, int n_points,
+              const uint32_t* col_offset, float noise_var, float llr_gain, int16_t* out);
+
+/* Mapper: codeword N/8 bytes -> xfec complex symbols (re, im pairs). */
+int orc_map(const uint8_t* cw, int B, int cw_bytes, int xfec, int n_mod, const uint32_t* col_offset,
+            int stride, const float* pts_re, const float* pts_im, float* sym);
+
+/* Known-answer hook: reference ldpc_make_bnl_update (message clamp, delta). */
+int orc_bnl_update(int raw_new, int old, int32_t* delta);
+
+/* The exp/log used by the log-MAP demapper (shared with the CUDA kernel's
+ * algorithm, exposed for accuracy tests). */
+float orc_exp_neg(float x);
+float orc_log(float x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,148 @@
+"""ctypes binding of the CPU oracle (test infrastructure; see oracle/fec_oracle.h).
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg.  The product package never imports it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+_lib = None
+_ref = None
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        import sys
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import build as _b  # oracle/build.py
+        sys.path.pop(0)
+        path = _b.build_oracle()
+        _lib = ctypes.CDLL(path)
+        _lib.orc_exp_neg.restype = ctypes.c_float
+        _lib.orc_exp_neg.argtypes = [ctypes.c_float]
+        _lib.orc_log.restype = ctypes.c_float
+        _lib.orc_log.argtypes = [ctypes.c_float]
+    return _lib
+
+
+def ref():
+    """The reference's own host code (oracle/_ref), or None when absent."""
+    global _ref
+    if _ref is None:
+        import sys
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import build as _b
+        sys.path.pop(0)
+        path = None
+        try:
+            path = _b.build_ref()
+        except Exception:
+            path = None
+        if path is None:
+            return None
+        _ref = ctypes.CDLL(path)
+    return _ref
+
+
+def code_info(fs, rate):
+    out = np.zeros(10, np.int32)
+    if lib().orc_code_info(fs, rate, _p(out, ctypes.c_int32)) != 0:
+        raise ValueError("unsupported code")
+    keys = ["N", "K", "q", "n_steps", "k_bch", "n_bch", "t", "p", "links_total", "cnl"]
+    return dict(zip(keys, (int(x) for x in out)))
+
+
+def ldpc_decode(fs, rate, llr, max_trials, weights=None, nthreads=8):
+    info = code_info(fs, rate)
+    llr = np.ascontiguousarray(llr, np.int16).reshape(-1, info["N"])
+    B = llr.shape[0]
+    hard = np.zeros((B, info["K"] // 8), np.uint8)
+    trials = np.zeros(B, np.int32)
+    w = None if weights is None else _p(np.ascontiguousarray(weights, np.int16), ctypes.c_int16)
+    rc = lib().orc_ldpc_decode(fs, rate, _p(llr, ctypes.c_int16), B, max_trials, w,
+                               _p(hard, ctypes.c_uint8), _p(trials, ctypes.c_int32), nthreads)
+    assert rc == 0
+    return hard, trials
+
+
+def syndrome_ok(fs, rate, llr):
+    llr = np.ascontiguousarray(llr, np.int16)
+    return bool(lib().orc_syndrome_ok(fs, rate, _p(llr, ctypes.c_int16)))
+
+
+def ldpc_encode(fs, rate, info_bytes):
+    info = code_info(fs, rate)
+    info_bytes = np.ascontiguousarray(info_bytes, np.uint8).reshape(-1, info["K"] // 8)
+    B = info_bytes.shape[0]
+    cw = np.zeros((B, info["N"] // 8), np.uint8)
+    assert lib().orc_ldpc_encode(fs, rate, _p(info_bytes, ctypes.c_uint8), _p(cw, ctypes.c_uint8), B) == 0
+    return cw
+
+
+def bch_generator(fs, rate):
+    g = np.zeros(4, np.uint64)
+    p = lib().orc_bch_generator(fs, rate, _p(g, ctypes.c_uint64))
+    return g, p
+
+
+def bch_encode(fs, rate, msg):
+    info = code_info(fs, rate)
+    msg = np.ascontiguousarray(msg, np.uint8).reshape(-1, info["k_bch"] // 8)
+    B = msg.shape[0]
+    cw = np.zeros((B, info["n_bch"] // 8), np.uint8)
+    assert lib().orc_bch_encode(fs, rate, _p(msg, ctypes.c_uint8), _p(cw, ctypes.c_uint8), B) == 0
+    return cw
+
+
+def bch_check(fs, rate, cw):
+    info = code_info(fs, rate)
+    cw = np.ascontiguousarray(cw, np.uint8).reshape(-1, info["n_bch"] // 8)
+    B = cw.shape[0]
+    rem = np.zeros((B, info["p"] // 8), np.uint8)
+    valid = np.zeros(B, np.int32)
+    assert lib().orc_bch_check(fs, rate, _p(cw, ctypes.c_uint8), _p(rem, ctypes.c_uint8),
+                               _p(valid, ctypes.c_int32), B) == 0
+    return rem, valid
+
+
+def demap(sym, xfec, interleaved_len, fec_len, n_mod, kind, pts, col, noise_var, llr_gain):
+    sym = np.ascontiguousarray(sym, np.float32).reshape(-1, xfec * 2)
+    B = sym.shape[0]
+    pts = np.asarray(pts, np.complex64)
+    pre = np.ascontiguousarray(pts.real, np.float32)
+    pim = np.ascontiguousarray(pts.imag, np.float32)
+    col = np.ascontiguousarray(np.asarray(col, np.uint32).reshape(8))
+    out = np.zeros((B, fec_len), np.int16)
+    assert lib().orc_demap(_p(sym, ctypes.c_float), B, xfec, interleaved_len, fec_len, n_mod, kind,
+                           _p(pre, ctypes.c_float), _p(pim, ctypes.c_float), len(pts),
+                           _p(col, ctypes.c_uint32), ctypes.c_float(noise_var),
+                           ctypes.c_float(llr_gain), _p(out, ctypes.c_int16)) == 0
+    return out
+
+
+def map_symbols(cw, xfec, n_mod, col, stride, pts):
+    cw = np.ascontiguousarray(cw, np.uint8)
+    B = cw.shape[0]
+    pts = np.asarray(pts, np.complex64)
+    pre = np.ascontiguousarray(pts.real, np.float32)
+    pim = np.ascontiguousarray(pts.imag, np.float32)
+    col = np.ascontiguousarray(np.asarray(col, np.uint32).reshape(8))
+    sym = np.zeros((B, xfec * 2), np.float32)
+    assert lib().orc_map(_p(cw, ctypes.c_uint8), B, cw.shape[1], xfec, n_mod, _p(col, ctypes.c_uint32),
+                         stride, _p(pre, ctypes.c_float), _p(pim, ctypes.c_float),
+                         _p(sym, ctypes.c_float)) == 0
+    return sym
+
+
+def bnl_update(raw, old):
+    d = np.zeros(1, np.int32)
+    m = lib().orc_bnl_update(raw, old, _p(d, ctypes.c_int32))
+    return m, int(d[0])
