@@ -1,0 +1,273 @@
+// cusat_fec.hpp -- header-only C++ shims with the reference's class names and
+// signatures, over the C ABI of cusat_fec.h.  A translation unit of the
+// reference's RX chain that includes this header instead of
+//   lib/cusat_dsp/cuda/ldpc_decode_kernel.cuh   (cuda::ldpc_decode_cuda)
+//   lib/cusat_dsp/ldpc_decode.h                 (ldpc_decode)
+//   lib/cusat_dsp/cuda/demapper_kernel.cuh      (cuda::demapper_cuda)
+//   lib/cusat_dsp/cuda/bch_check_kernel.cuh     (cuda::bch_check_cuda)
+// compiles unchanged and links against libcusat_fec.so.
+//
+// Error behaviour mirrors the reference: a batch size outside 1..max_batch is
+// a silent no-op (ldpc_decode_kernel.cu:1291-1292, demapper_kernel.cu:305-306),
+// a CUDA failure aborts (cuda_util.cu:23-44), the BCH checker throws
+// std::invalid_argument on a bad geometry, negative batch or null buffer
+// (bch_check_kernel.cu:17-18,28-33), and construction without a GPU aborts
+// (ldpc_decode.cc:33-40).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+#include <stdexcept>
+
+#include "cusat_fec.h"
+
+#ifndef INCLUDED_CUSAT_DSP_MODCOD_TYPES_H
+// Standalone use: the enumerations of the reference's modcod_types.h with
+// the same numeric values (cusat_data.h lists all of them).
+namespace cusat_dsp {
+enum code_rate_t : int {
+    RATE_1_4, RATE_1_3, RATE_2_5, RATE_1_2, RATE_3_5, RATE_2_3, RATE_3_4, RATE_4_5, RATE_5_6, RATE_8_9,
+    RATE_9_10, RATE_11_45, RATE_4_15, RATE_13_45, RATE_14_45, RATE_9_20, RATE_7_15, RATE_90_180,
+    RATE_8_15, RATE_96_180, RATE_11_20, RATE_100_180, RATE_26_45, RATE_104_180, RATE_18_30,
+    RATE_28_45, RATE_23_36, RATE_116_180, RATE_20_30, RATE_124_180, RATE_25_36, RATE_32_45,
+    RATE_128_180, RATE_13_18, RATE_22_30, RATE_132_180, RATE_135_180, RATE_7_9, RATE_140_180,
+    RATE_154_180,
+};
+enum fecframe_size_t : int { FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM };
+enum modulation_t : int { MOD_QPSK, MOD_8PSK, MOD_8APSK, MOD_16APSK, MOD_32APSK, MOD_64APSK, MOD_128APSK,
+                          MOD_256APSK };
+// Flat table descriptor (reference ldpc_tables/ldpc_code.h:25-39); only n
+// is read here, to recover the frame size.
+struct ldpc_code {
+    int n, k, m, links_total, links_max_cn, n_rows;
+    const uint8_t* row_deg;
+    const uint32_t* row_off;
+    const uint16_t* addr;
+};
+}  // namespace cusat_dsp
+#endif
+
+namespace cusat_dsp {
+namespace cusat_shim {
+
+inline void die(int rc, const char* what)
+{
+    fprintf(stderr, "cusat_fec: %s failed (%d): %s\n", what, rc, cusat_last_error());
+    abort();
+}
+
+inline int framesize_of(int n_bits)
+{
+    return n_bits == 64800 ? FECFRAME_NORMAL : n_bits == 16200 ? FECFRAME_SHORT : FECFRAME_MEDIUM;
+}
+
+}  // namespace cusat_shim
+
+namespace cuda {
+
+// Reference lib/cusat_dsp/cuda/ldpc_decode_kernel.cuh:22-107.
+class ldpc_decode_cuda
+{
+  public:
+    ldpc_decode_cuda(const ldpc_code* code, code_rate_t rate, int max_trials = 25, int max_batch = 64)
+    {
+        const int rc = cusat_ldpc_decoder_create(cusat_shim::framesize_of(code->n), (int)rate, max_trials,
+                                                 max_batch, &d_);
+        if (rc)
+            cusat_shim::die(rc, "ldpc_decode_cuda");
+        int32_t info[8];
+        cusat_ldpc_decoder_info(d_, info);
+        n_ = info[0];
+        k_ = info[1];
+        max_batch_ = max_batch;
+    }
+    ~ldpc_decode_cuda() { cusat_ldpc_decoder_destroy(d_); }
+    ldpc_decode_cuda(const ldpc_decode_cuda&) = delete;
+    ldpc_decode_cuda& operator=(const ldpc_decode_cuda&) = delete;
+
+    void decode_batch(const int16_t* soft_in, uint8_t* hard_out, int* trials_out, int batch_size,
+                      cudaStream_t stream)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_ldpc_decode_batch(d_, soft_in, hard_out, (int32_t*)trials_out, batch_size, stream);
+        if (rc)
+            cusat_shim::die(rc, "decode_batch");
+    }
+
+    void decode_batch_d2h(const int16_t* soft_in_dev, uint8_t* hard_out_host, int* trials_out_host,
+                          int batch_size, cudaStream_t stream)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_ldpc_decode_batch_d2h(d_, soft_in_dev, hard_out_host, (int32_t*)trials_out_host,
+                                                   batch_size, stream);
+        if (rc)
+            cusat_shim::die(rc, "decode_batch_d2h");
+    }
+
+    void decode_launch_async(const int16_t* soft_in, int batch_size, cudaStream_t stream,
+                             uint8_t* hard_out = nullptr, int* result_out = nullptr)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_ldpc_decode_launch(d_, soft_in, batch_size, stream, hard_out, (int32_t*)result_out);
+        if (rc)
+            cusat_shim::die(rc, "decode_launch_async");
+    }
+
+    int n_bits() const { return n_; }
+    int k_bits() const { return k_; }
+    int k_bytes() const { return k_ / 8; }
+
+  private:
+    cusat_ldpc_decoder* d_ = nullptr;
+    int n_ = 0, k_ = 0, max_batch_ = 0;
+};
+
+// Reference lib/cusat_dsp/cuda/demapper_kernel.cuh:23-89.
+class demapper_cuda
+{
+  public:
+    demapper_cuda(modulation_t constellation, code_rate_t rate, fecframe_size_t framesize, int max_batch = 64)
+    {
+        const int rc = cusat_demapper_create((int)constellation, (int)rate, (int)framesize, max_batch, &d_);
+        if (rc)
+            cusat_shim::die(rc, "demapper_cuda");
+        cusat_demapper_info(d_, info_);
+        max_batch_ = max_batch;
+    }
+    ~demapper_cuda() { cusat_demapper_destroy(d_); }
+    demapper_cuda(const demapper_cuda&) = delete;
+    demapper_cuda& operator=(const demapper_cuda&) = delete;
+
+    void demap_batch(const float* sym_in_host, int batch_size, float noise_var, float llr_gain)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_demap_batch(d_, sym_in_host, batch_size, noise_var, llr_gain);
+        if (rc)
+            cusat_shim::die(rc, "demap_batch");
+    }
+
+    void demap_batch_async(const float* sym_in_host, int batch_size, float noise_var, float llr_gain,
+                           cudaStream_t stream)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_demap_batch_async(d_, sym_in_host, batch_size, noise_var, llr_gain, stream);
+        if (rc)
+            cusat_shim::die(rc, "demap_batch_async");
+    }
+
+    float capped_llr_gain(float llr_gain) const { return cusat_demapper_capped_llr_gain(d_, llr_gain); }
+    int16_t* soft_out_dev() const { return cusat_demapper_soft_out_dev(d_); }
+    int fecframe_len() const { return info_[0]; }
+    int xfecframe_len() const { return info_[1]; }
+    int n_mod() const { return info_[2]; }
+
+  private:
+    cusat_demapper* d_ = nullptr;
+    int32_t info_[4] = {0, 0, 0, 0};
+    int max_batch_ = 0;
+};
+
+// Reference lib/cusat_dsp/cuda/bch_check_kernel.cuh:9-24.
+class bch_check_cuda
+{
+  public:
+    bch_check_cuda(const uint64_t* flat_lut, const uint64_t* gen_poly, int gen_degree, unsigned int n_bytes)
+    {
+        const int rc = cusat_bch_checker_create(flat_lut, gen_poly, gen_degree, n_bytes, &c_);
+        if (rc == CUSAT_ERR_ARG)
+            throw std::invalid_argument(cusat_last_error());
+        if (rc)
+            cusat_shim::die(rc, "bch_check_cuda");
+    }
+    ~bch_check_cuda() { cusat_bch_checker_destroy(c_); }
+    bch_check_cuda(const bch_check_cuda&) = delete;
+    bch_check_cuda& operator=(const bch_check_cuda&) = delete;
+
+    void check_async(const uint8_t* codewords_dev, int* valid_out_dev, int batch_size, cudaStream_t stream)
+    {
+        if (batch_size < 0)
+            throw std::invalid_argument("negative BCH batch");
+        if (!batch_size)
+            return;
+        if (!codewords_dev || !valid_out_dev)
+            throw std::invalid_argument("null BCH checker buffer");
+        const int rc = cusat_bch_check_launch(c_, codewords_dev, (int32_t*)valid_out_dev, nullptr, batch_size,
+                                              stream);
+        if (rc)
+            cusat_shim::die(rc, "check_async");
+    }
+    unsigned int n_bytes() const { return cusat_bch_checker_n_bytes(c_); }
+
+  private:
+    cusat_bch_checker* c_ = nullptr;
+};
+
+}  // namespace cuda
+
+// Reference lib/cusat_dsp/ldpc_decode.h:22-69: owns its stream.
+class ldpc_decode
+{
+  public:
+    ldpc_decode(fecframe_size_t framesize, code_rate_t rate, int max_trials = 25, int cuda_max_batch = 64)
+    {
+        const int rc = cusat_ldpc_decoder_create((int)framesize, (int)rate, max_trials, cuda_max_batch, &d_);
+        if (rc)
+            cusat_shim::die(rc, "ldpc_decode");
+        int32_t info[8];
+        cusat_ldpc_decoder_info(d_, info);
+        n_ = (unsigned)info[0];
+        k_ = (unsigned)info[1];
+        max_batch_ = cuda_max_batch;
+        if (cudaStreamCreate(&stream_) != cudaSuccess)
+            cusat_shim::die(CUSAT_ERR_CUDA, "cudaStreamCreate");
+    }
+    ~ldpc_decode()
+    {
+        cusat_ldpc_decoder_destroy(d_);
+        if (stream_)
+            cudaStreamDestroy(stream_);
+    }
+    ldpc_decode(const ldpc_decode&) = delete;
+    ldpc_decode& operator=(const ldpc_decode&) = delete;
+
+    void decode_batch_cuda(const int16_t* soft_in, uint8_t* hard_out, int* trials_out, int batch_size)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_ldpc_decode_batch(d_, soft_in, hard_out, (int32_t*)trials_out, batch_size, stream_);
+        if (rc)
+            cusat_shim::die(rc, "decode_batch_cuda");
+    }
+
+    void decode_batch_cuda_d2h(const int16_t* soft_in_dev, uint8_t* hard_out, int* trials_out, int batch_size)
+    {
+        if (batch_size <= 0 || batch_size > max_batch_)
+            return;
+        const int rc = cusat_ldpc_decode_batch_d2h(d_, soft_in_dev, hard_out, (int32_t*)trials_out, batch_size,
+                                                   stream_);
+        if (rc)
+            cusat_shim::die(rc, "decode_batch_cuda_d2h");
+    }
+
+    CUstream_st* cuda_stream() const { return stream_; }
+    unsigned int n_bits() const { return n_; }
+    unsigned int k_bits() const { return k_; }
+    unsigned int n_bytes() const { return n_ / 8; }
+    unsigned int k_bytes() const { return k_ / 8; }
+
+  private:
+    cusat_ldpc_decoder* d_ = nullptr;
+    cudaStream_t stream_ = nullptr;
+    unsigned n_ = 0, k_ = 0;
+    int max_batch_ = 0;
+};
+
+}  // namespace cusat_dsp
