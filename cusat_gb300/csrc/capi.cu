@@ -54,18 +54,24 @@ struct DevPlan {
 
 int upload_plan(const cusat::CodePlan& p, DevPlan* d)
 {
-    const size_t n_circ = p.circ.size() * 4, n_cnt = p.cnt.size(), n_sched = p.sched.size() * 2,
-                 n_conf = p.step_conf.size();
-    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    const size_t o_circ = 0, o_cnt = al(n_circ), o_sched = o_cnt + al(n_cnt), o_conf = o_sched + al(n_sched);
-    const size_t total = o_conf + al(n_conf);
-    std::vector<unsigned char> h(total, 0);
-    memcpy(&h[o_circ], p.circ.data(), n_circ);
-    memcpy(&h[o_cnt], p.cnt.data(), n_cnt);
-    memcpy(&h[o_sched], p.sched.data(), n_sched);
-    memcpy(&h[o_conf], p.step_conf.data(), n_conf);
-    CU(cudaMalloc(&d->blob, total), "cudaMalloc(plan)");
-    CU(cudaMemcpy(d->blob, h.data(), total, cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
+    struct Part { const void* src; size_t n; size_t off; };
+    Part parts[] = {
+        {p.tab.data(), p.tab.size() * 4, 0},         {p.cnt.data(), p.cnt.size(), 0},
+        {p.n_plain.data(), p.n_plain.size(), 0},     {p.n_pg.data(), p.n_pg.size(), 0},
+        {p.sched.data(), p.sched.size() * 2, 0},     {p.step_conf.data(), p.step_conf.size(), 0},
+        {p.own_off.data(), p.own_off.size() * 2, 0}, {p.own.data(), p.own.size() * 4, 0},
+    };
+    size_t total = 0;
+    for (auto& pt : parts) {
+        pt.off = total;
+        total += (pt.n + 255) & ~(size_t)255;
+    }
+    std::vector<unsigned char> h(total + 256, 0);
+    for (auto& pt : parts)
+        if (pt.n)
+            memcpy(&h[pt.off], pt.src, pt.n);
+    CU(cudaMalloc(&d->blob, total + 256), "cudaMalloc(plan)");
+    CU(cudaMemcpy(d->blob, h.data(), total + 256, cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
     unsigned char* b = (unsigned char*)d->blob;
     cusat::DevCode& c = d->code;
     c.N = p.N;
@@ -76,10 +82,15 @@ int upload_plan(const cusat::CodePlan& p, DevPlan* d)
     c.cmax = p.cmax;
     c.fast_lim = p.fast_lim;
     c.msg_row = p.msg_row;
-    c.circ = (const uint32_t*)(b + o_circ);
-    c.cnt = (const uint8_t*)(b + o_cnt);
-    c.sched = (const int16_t*)(b + o_sched);
-    c.step_conf = (const uint8_t*)(b + o_conf);
+    c.n_own = (int)(p.own.size() / 2);
+    c.tab = (const uint2*)(b + parts[0].off);
+    c.cnt = b + parts[1].off;
+    c.n_plain = b + parts[2].off;
+    c.n_pg = b + parts[3].off;
+    c.sched = (const int16_t*)(b + parts[4].off);
+    c.step_conf = b + parts[5].off;
+    c.own_off = (const uint16_t*)(b + parts[6].off);
+    c.own = (const uint2*)(b + parts[7].off);
     return CUSAT_OK;
 }
 

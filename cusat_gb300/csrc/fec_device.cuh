@@ -15,10 +15,15 @@ struct DevCode {
     int cmax;        // circulant slots per layer in the tables (= kernel CMAX)
     int fast_lim;    // |LLR| bound under which no int16 saturation can occur
     int msg_row;     // bytes of one check row of messages (16 or 32)
-    const uint32_t* circ;      // [q * cmax]
-    const uint8_t* cnt;        // [q]
-    const int16_t* sched;      // [n_steps * 2]
-    const uint8_t* step_conf;  // [n_steps] 1 if the step has a shared variable node
+    int n_own;       // owner items over all steps
+    const uint2* tab;          // [q * cmax] slot descriptors (fec_consts.h)
+    const uint8_t* cnt;        // [q] circulants per layer
+    const uint8_t* n_plain;    // [q] plain circulants (first in the layer)
+    const uint8_t* n_pg;       // [q] plain + guest circulants
+    const int16_t* sched;      // [n_steps * 2] layer per lane, -1 idle
+    const uint8_t* step_conf;  // [n_steps] 1 if the step has owner items
+    const uint16_t* own_off;   // [n_steps + 1] owner items of step s
+    const uint2* own;          // [n_own]
 };
 
 // Demapper parameters of one MODCOD (points live in device memory).

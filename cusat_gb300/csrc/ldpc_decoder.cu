@@ -38,21 +38,20 @@ int decoder_threads(int lanes) { return lanes * kLaneThreads; }
 void decoder_smem_layout(DecodeArgs* a, int cmax, int n_points)
 {
     const DevCode& c = a->code;
-    int off = align16(c.N * 2);
-    a->sm_stage = off;
-    off = align16(off + kMaxStage * kM * 2);
-    a->sm_circ = off;
-    off = align16(off + c.q * cmax * 4);
-    a->sm_sched = off;
-    off = align16(off + c.n_steps * 4);
-    a->sm_cnt = off;
-    off = align16(off + c.q);
-    a->sm_conf = off;
-    off = align16(off + c.n_steps);
-    a->sm_pts = off;
-    off = align16(off + n_points * 8);
-    a->sm_misc = off;
-    off = align16(off + 16);
+    int off = align16(c.N * 2 + 2);  // APP + the absent-edge scratch slot
+    auto take = [&](int* field, int bytes) {
+        *field = off;
+        off = align16(off + bytes);
+    };
+    take(&a->sm_stage, kMaxStage * kM * 4);
+    take(&a->sm_tab, c.q * cmax * 8);
+    take(&a->sm_sched, c.n_steps * 4);
+    take(&a->sm_lay, c.q * 4);
+    take(&a->sm_conf, c.n_steps);
+    take(&a->sm_own_off, (c.n_steps + 1) * 2);
+    take(&a->sm_own, c.n_own * 8);
+    take(&a->sm_pts, n_points * 8);
+    take(&a->sm_misc, 16);
     a->sm_total = off;
 }
 

@@ -9,30 +9,33 @@
 // Frame state in shared memory: the int16 APP of the N bits, information
 // bits in natural order then the parity bits transposed to
 // [layer][check] (slot i*360 + j holds parity bit q*j + i).  Check j of
-// layer i reads information bit base + (j - shift) mod 360 of each
-// circulant: consecutive threads read consecutive halfwords, so every
-// gather and scatter is a conflict-free shared-memory access.  Check-to-bit
-// messages (int8) live in this CTA's global scratch, one 16- or 32-byte row
-// per check (two parity edges first, then the circulants), loaded with
-// 128-bit loads one step ahead of use.
+// layer i reads bit (j + r) mod 360 of each circulant's group, found with
+// one add and one unsigned DPX min (viaddmin): consecutive threads read
+// consecutive halfwords, so gathers and scatters are conflict-free
+// shared-memory accesses.  Check-to-bit messages (int8) live in this CTA's
+// global scratch, one 16- or 32-byte row per check (the two parity edges,
+// then the circulants), loaded with 128-bit loads one step ahead of use.
 //
 // Arithmetic.  The reference semantics (qsat16 extrinsic, offset min-sum
 // with beta 1, int8 clamp, saturating APP updates) are computed exactly.
-// When every channel LLR of the frame is within DevCode::fast_lim, no
-// intermediate can leave int16 (|APP| <= |llr| + 127 (deg + 1)), and the
-// kernel takes the SAT = false path that drops the clamps; otherwise the
-// SAT = true path evaluates every saturation.  Magnitudes are compared
-// before the offset: offset-then-clamp is monotone, so min1/min2 and the
-// "is this edge the minimum" test give the same messages as the
-// reference's finalp_oms_i16 (:242-275), ties included.
+// When every channel LLR of the frame is within DevCode::fast_lim no
+// intermediate can leave int16 (|APP| <= |llr| + 127 (deg + 1)) and the
+// kernel runs the SAT = false path without clamps; otherwise the SAT = true
+// path evaluates every saturation.  Magnitudes are compared before the
+// offset: offset-then-clamp is monotone, so min1/min2 and the "is this edge
+// the minimum" test give the messages of the reference's finalp_oms_i16
+// (:242-275), ties included.
 //
 // Checks of one step that share a variable node (a table row with two
 // accumulator addresses in one layer, or in both paired layers) are a data
-// race in the reference (:793-802).  Here they are resolved
-// deterministically, step-Jacobi: the first circulant on the node (owner)
-// keeps its updated value in a register, the others (guests) write their
-// message delta to a stage row, and after a CTA barrier the owner stores
+// race in the reference (:793-802).  They are resolved deterministically,
+// step-Jacobi: owner and guest circulants (fec_consts.h) write to stage rows
+// instead of the APP, and after a barrier the step's owner items store
 // sat16(APP + all deltas).
+//
+// Syndrome.  The check before each iteration (reference :693-745) votes
+// after the first step's checks and then every 4 steps, stopping at the
+// first failing group.
 #pragma once
 
 #include "fec_device.cuh"
@@ -52,7 +55,18 @@ struct DecodeArgs {
     unsigned int* queue;     // frame counter, zero at launch
     const int16_t* weights;  // learned min-sum weights or nullptr (plain)
     // shared-memory carve-up (bytes)
-    int sm_stage, sm_circ, sm_sched, sm_cnt, sm_conf, sm_pts, sm_misc, sm_total;
+    int sm_stage, sm_tab, sm_sched, sm_lay, sm_conf, sm_own_off, sm_own, sm_pts, sm_misc,
+        sm_total;
+};
+
+// Shared-memory views of the code tables.
+struct SmemCode {
+    const uint2* tab;
+    const int16_t* sched;
+    const uint32_t* lay;  // per layer: circulants | plain << 8 | plain+guest << 16
+    const uint8_t* conf;
+    const uint16_t* own_off;
+    const uint2* own;
 };
 
 __device__ __forceinline__ int sat16(int v) { return max(-32768, min(32767, v)); }
@@ -71,6 +85,13 @@ __device__ __forceinline__ uint32_t word_of(const uint4& v, int k)
     return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
 }
 
+// old message of edge e of a row held in registers
+template <int RW>
+__device__ __forceinline__ int row_byte(const uint4 (&row)[RW], int e)
+{
+    return sbyte(word_of(row[e >> 4], (e >> 2) & 3), e & 3);
+}
+
 template <int RW>
 __device__ __forceinline__ void load_row(uint4 (&dst)[RW], const uint4* src, bool pred)
 {
@@ -79,39 +100,53 @@ __device__ __forceinline__ void load_row(uint4 (&dst)[RW], const uint4* src, boo
         dst[w] = pred ? __ldcg(src + w) : make_uint4(0, 0, 0, 0);
 }
 
-// Syndrome of the current hard decisions: true iff every check is
-// satisfied.  Steps are voted in groups of 4 (one barrier per group), so a
-// failing frame pays about one group.  Reference :693-745.
-template <int CMAX, int LANES>
-__device__ bool syndrome_ok(const int16_t* app, const uint32_t* s_circ, const int16_t* s_sched,
-                            const uint8_t* s_cnt, int K, int q, int n_steps, int lane, int j,
-                            bool active)
+// (j + r) mod 360 for j, r in [0, 360)
+__device__ __forceinline__ int rot360(int j, uint32_t r)
 {
-    const int16_t* pty = app + K;
-    for (int s0 = 0; s0 < n_steps; s0 += 4) {
+    const unsigned u = (unsigned)j + r;
+    return (int)__viaddmin_u32(u, (unsigned)(-kM), u);
+}
+
+__device__ __forceinline__ int lds16(const unsigned char* smem, int off)
+{
+    return *reinterpret_cast<const int16_t*>(smem + off);
+}
+
+__device__ __forceinline__ void sts16(unsigned char* smem, int off, int v)
+{
+    *reinterpret_cast<int16_t*>(smem + off) = (int16_t)v;
+}
+
+// Syndrome of the current hard decisions: true iff every check is
+// satisfied.  The first vote (one barrier) follows the first step's checks,
+// the next ones groups of 4 steps, so a failing frame -- nearly every
+// iteration of every frame -- pays for about one step of gathers.
+template <int CMAX>
+__device__ bool syndrome_ok(const unsigned char* smem, const SmemCode& t, int K, int q, int n_steps, int lane,
+                            int j, bool active)
+{
+    const int pty = 2 * K;
+    for (int s0 = 0, g = 1; s0 < n_steps; s0 += g, g = 4) {
         int bad = 0;
         if (active) {
-            const int s1 = min(s0 + 4, n_steps);
+            const int s1 = min(s0 + g, n_steps);
             for (int s = s0; s < s1; s++) {
-                const int i = s_sched[2 * s + lane];
+                const int i = t.sched[2 * s + lane];
                 if (i < 0)
                     continue;
-                const int cnt = s_cnt[i];
-                int x = pty[i * kM + j];
+                const int cnt = (int)(t.lay[i] & 0xff);
+                int x = lds16(smem, pty + 2 * (i * kM + j));
                 if (i > 0)
-                    x ^= pty[(i - 1) * kM + j];
+                    x ^= lds16(smem, pty + 2 * ((i - 1) * kM + j));
                 else if (j > 0)
-                    x ^= pty[(q - 1) * kM + j - 1];
-                const uint32_t* ci = s_circ + i * CMAX;
+                    x ^= lds16(smem, pty + 2 * ((q - 1) * kM + j - 1));
+                const uint2* tb = t.tab + i * CMAX;
 #pragma unroll
-                for (int e = 0; e < CMAX; e++) {
+                for (int e = 0; e < CMAX; e++)
                     if (e < cnt) {
-                        const uint32_t w = ci[e];
-                        int m = j - (int)((w >> 16) & 0x1ff);
-                        m += (m >> 31) & kM;
-                        x ^= app[(int)(w & 0xffff) + m];
+                        const uint2 w = tb[e];
+                        x ^= lds16(smem, (int)w.x + 2 * rot360(j, w.y & 0xffff));
                     }
-                }
                 bad |= x;
             }
         }
@@ -145,9 +180,99 @@ __device__ __forceinline__ int scaled_mag(int r, int beta, int alpha)
     return min(m, 127);
 }
 
+// One check row of one layer: gather, offset min-sum, scatter, new message
+// row.  GENERAL handles layers with fewer circulants than CMAX or with
+// owner/guest circulants; the other instantiation is straight-line code for
+// the common layer whose CMAX circulants are all plain.
+template <int CMAX, int RW, bool SAT, bool GENERAL>
+__device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char* smem, int32_t* stage,
+                                              const uint2* tb, uint32_t lay, int j, int ps0, int ps1,
+                                              bool absent, const uint4 (&cur)[RW], uint4* dst, int trial)
+{
+    constexpr int NE = CMAX + 2;
+    const int cnt = GENERAL ? (int)(lay & 0xff) : CMAX;
+    const int np = GENERAL ? (int)((lay >> 8) & 0xff) : CMAX;
+    const int npg = GENERAL ? (int)((lay >> 16) & 0xff) : CMAX;
+    int d[NE];
+    int ad[CMAX];
+    // gather: two parity edges (the second absent for check 0 of layer 0,
+    // which then reads and writes a dummy slot), then the circulants
+    const int a0 = lds16(smem, ps0);
+    const int a1 = lds16(smem, ps1);
+    {
+        const int x0 = a0 - row_byte(cur, 0);
+        const int x1 = a1 - row_byte(cur, 1);
+        d[0] = SAT ? sat16(x0) : x0;
+        d[1] = absent ? kBig : (SAT ? sat16(x1) : x1);
+    }
+#pragma unroll
+    for (int e = 0; e < CMAX; e++) {
+        if (!GENERAL || e < cnt) {
+            const uint2 w = tb[e];
+            ad[e] = (int)w.x + 2 * rot360(j, w.y & 0xffff);
+            const int x = lds16(smem, ad[e]) - row_byte(cur, e + 2);
+            d[2 + e] = SAT ? sat16(x) : x;
+        } else {
+            ad[e] = 0;
+            d[2 + e] = kBig;
+        }
+    }
+    // check node: min1/min2 of |extrinsic|, sign product
+    int r1 = kBig, r2 = kBig, sx = 0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+        const int r = abs(d[e]);
+        r2 = min(r2, max(r1, r));
+        r1 = min(r1, r);
+        sx ^= d[e];
+    }
+    int m1, m2;
+    if (a.weights) {
+        const int deg = cnt + (absent ? 1 : 2);
+        const int16_t* w = a.weights + ((size_t)trial * 32 + deg) * 2;
+        m1 = scaled_mag(r1, w[0], w[1]);
+        m2 = scaled_mag(r2, w[0], w[1]);
+    } else {
+        m1 = min(max(r1 - 1, 0), 127);
+        m2 = min(max(r2 - 1, 0), 127);
+    }
+    // each message carries the sign product of the other edges
+    const int sg = sx >> 31;
+    const int p1 = (m1 ^ sg) - sg, p2 = (m2 ^ sg) - sg;
+    uint32_t wv[RW * 4];
+#pragma unroll
+    for (int k = 0; k < RW * 4; k++)
+        wv[k] = 0;
+#pragma unroll
+    for (int e = 0; e < NE; e++) {
+        const int ds = d[e] >> 31;
+        const int mg = (((abs(d[e]) == r1) ? p2 : p1) ^ ds) - ds;
+        wv[e >> 2] = __byte_perm(wv[e >> 2], (uint32_t)mg,
+                                 (e & 3) == 0 ? 0x3214 : (e & 3) == 1 ? 0x3240 : (e & 3) == 2 ? 0x3410 : 0x4210);
+        if (e < 2) {
+            // parity: APP = sat16(extrinsic + message)
+            sts16(smem, e == 0 ? ps0 : ps1, SAT ? sat16(d[e] + mg) : d[e] + mg);
+        } else if (!GENERAL || e - 2 < cnt) {
+            const int o = e - 2;
+            // SAT: re-read the APP (no other check of the step writes this
+            // bit before the barrier) and saturate once
+            const int nv = SAT ? lds16(smem, ad[o]) + mg - row_byte(cur, e) : d[e] + mg;
+            if (!GENERAL || o < np) {
+                sts16(smem, ad[o], SAT ? sat16(nv) : nv);
+            } else {
+                const uint2 w = tb[o];
+                const int m = (ad[o] - (int)w.x) >> 1;
+                stage[(int)(w.y >> 16) * kM + m] = o < npg ? mg - row_byte(cur, e) : nv;
+            }
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < RW; w++)
+        __stcg(dst + w, make_uint4(wv[4 * w], wv[4 * w + 1], wv[4 * w + 2], wv[4 * w + 3]));
+}
+
 template <int CMAX, int LANES, bool SAT>
-__device__ void decode_frame(const DecodeArgs& a, int16_t* app, int16_t* stage, const uint32_t* s_circ,
-                             const int16_t* s_sched, const uint8_t* s_cnt, const uint8_t* s_conf, int f)
+__device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, int32_t* stage, const SmemCode& t, int f)
 {
     constexpr int NE = CMAX + 2;
     constexpr int RW = (NE + 15) / 16;
@@ -157,11 +282,13 @@ __device__ void decode_frame(const DecodeArgs& a, int16_t* app, int16_t* stage, 
     const int j = tid - lane * kLaneThreads;
     const bool active = j < kM;
     const int K = c.K, q = c.q, T = a.max_trials, n_steps = c.n_steps;
+    const int pty = 2 * K;         // byte offset of the parity APP
+    const int dummy = 2 * c.N;     // scratch slot for the absent parity edge
     uint4* msg_cta = a.msg + (size_t)blockIdx.x * ((size_t)c.R * RW);
     int result = -1;
 
     for (int trial = 0;; trial++) {
-        if (syndrome_ok<CMAX, LANES>(app, s_circ, s_sched, s_cnt, K, q, n_steps, lane, j, active)) {
+        if (syndrome_ok<CMAX>(smem, t, K, q, n_steps, lane, j, active)) {
             result = T - trial;
             break;
         }
@@ -170,133 +297,42 @@ __device__ void decode_frame(const DecodeArgs& a, int16_t* app, int16_t* stage, 
         const bool load = trial > 0;
         uint4 cur[RW];
         {
-            const int i0 = s_sched[lane];
+            const int i0 = t.sched[lane];
             load_row<RW>(cur, msg_cta + ((size_t)max(i0, 0) * kM + j) * RW, load && active && i0 >= 0);
         }
         for (int s = 0; s < n_steps; s++) {
-            const int i = s_sched[2 * s + lane];
+            const int i = t.sched[2 * s + lane];
             uint4 nxt[RW];
             {
-                const int i_n = s + 1 < n_steps ? s_sched[2 * (s + 1) + lane] : -1;
-                load_row<RW>(nxt, msg_cta + ((size_t)max(i_n, 0) * kM + j) * RW,
-                             load && active && i_n >= 0);
+                const int i_n = s + 1 < n_steps ? t.sched[2 * (s + 1) + lane] : -1;
+                load_row<RW>(nxt, msg_cta + ((size_t)max(i_n, 0) * kM + j) * RW, load && active && i_n >= 0);
             }
-            const bool work = active && i >= 0;
-            // keep the bit indices of the circulants in registers when they fit
-            constexpr bool KEEP_VN = CMAX <= 14;
-            int dd[NE];
-            int vn[KEEP_VN ? CMAX : 1];
-            int cnt = 0;
-            const uint32_t* ci = s_circ + max(i, 0) * CMAX;
-            if (work) {
-                cnt = s_cnt[i];
-                // gather: two parity edges, then the circulants
-                const int ps0 = K + i * kM + j;
-                const int ps1 = i > 0 ? ps0 - kM : (j > 0 ? K + (q - 1) * kM + j - 1 : -1);
-                {
-                    const int a0 = app[ps0] - sbyte(cur[0].x, 0);
-                    dd[0] = SAT ? sat16(a0) : a0;
-                    if (ps1 >= 0) {
-                        const int a1 = app[ps1] - sbyte(cur[0].x, 1);
-                        dd[1] = SAT ? sat16(a1) : a1;
-                    } else {
-                        dd[1] = kBig;
-                    }
-                }
-#pragma unroll
-                for (int e = 0; e < CMAX; e++) {
-                    if (e < cnt) {
-                        const uint32_t w = ci[e];
-                        int m = j - (int)((w >> 16) & 0x1ff);
-                        m += (m >> 31) & kM;
-                        const int v = (int)(w & 0xffff) + m;
-                        if (KEEP_VN)
-                            vn[KEEP_VN ? e : 0] = v;
-                        const int x = app[v] - sbyte(word_of(cur[(e + 2) >> 4], ((e + 2) >> 2) & 3), (e + 2) & 3);
-                        dd[2 + e] = SAT ? sat16(x) : x;
-                    } else {
-                        dd[2 + e] = kBig;
-                    }
-                }
-                // check node: min1/min2 of |extrinsic|, sign product
-                int r1 = kBig, r2 = kBig, sx = 0;
-#pragma unroll
-                for (int e = 0; e < NE; e++) {
-                    const int r = abs(dd[e]);
-                    r2 = min(r2, max(r1, r));
-                    r1 = min(r1, r);
-                    sx ^= dd[e];
-                }
-                int m1, m2;
-                if (a.weights) {
-                    const int deg = cnt + (ps1 >= 0 ? 2 : 1);
-                    const int16_t* w = a.weights + ((size_t)trial * 32 + deg) * 2;
-                    m1 = scaled_mag(r1, w[0], w[1]);
-                    m2 = scaled_mag(r2, w[0], w[1]);
-                } else {
-                    m1 = min(max(r1 - 1, 0), 127);
-                    m2 = min(max(r2 - 1, 0), 127);
-                }
-                // messages, scatter, and the new message row
-                uint32_t wv[RW * 4];
-#pragma unroll
-                for (int k = 0; k < RW * 4; k++)
-                    wv[k] = 0;
-#pragma unroll
-                for (int e = 0; e < NE; e++) {
-                    const int oth = (abs(dd[e]) == r1) ? m2 : m1;
-                    const int mg = ((sx ^ dd[e]) < 0) ? -oth : oth;
-                    wv[e >> 2] = __byte_perm(wv[e >> 2], (uint32_t)mg,
-                                             (e & 3) == 0 ? 0x3214 : (e & 3) == 1 ? 0x3240
-                                                                   : (e & 3) == 2 ? 0x3410 : 0x4210);
-                    if (e == 0) {
-                        app[ps0] = (int16_t)(SAT ? sat16(dd[0] + mg) : dd[0] + mg);
-                    } else if (e == 1) {
-                        if (ps1 >= 0)
-                            app[ps1] = (int16_t)(SAT ? sat16(dd[1] + mg) : dd[1] + mg);
-                    } else if (e - 2 < cnt) {
-                        const uint32_t w = ci[e - 2];
-                        int v;
-                        if (KEEP_VN) {
-                            v = vn[KEEP_VN ? e - 2 : 0];
-                        } else {
-                            int m = j - (int)((w >> 16) & 0x1ff);
-                            m += (m >> 31) & kM;
-                            v = (int)(w & 0xffff) + m;
-                        }
-                        const int delta = mg - sbyte(word_of(cur[e >> 4], (e >> 2) & 3), e & 3);
-                        // SAT: re-read the APP (unchanged: no other check of
-                        // the step writes this bit) and saturate once
-                        const int nv = SAT ? app[v] + delta : dd[e] + mg;
-                        const uint32_t role = (w >> 25) & 3;
-                        if (role == kRolePlain)
-                            app[v] = (int16_t)(SAT ? sat16(nv) : nv);
-                        else if (role == kRoleGuest)
-                            stage[((w >> 27) & 7) * kM + (v - (int)(w & 0xffff))] = (int16_t)delta;
-                        else
-                            dd[e] = nv;  // owner: completed after the barrier
-                    }
-                }
+            if (active && i >= 0) {
+                const uint32_t lay = t.lay[i];
+                const int ps0 = pty + 2 * (i * kM + j);
+                const bool absent = (i == 0 && j == 0);
+                const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? dummy : pty + 2 * ((q - 1) * kM + j - 1));
+                const uint2* tb = t.tab + i * CMAX;
                 uint4* dst = msg_cta + ((size_t)i * kM + j) * RW;
-#pragma unroll
-                for (int w = 0; w < RW; w++)
-                    __stcg(dst + w, make_uint4(wv[4 * w], wv[4 * w + 1], wv[4 * w + 2], wv[4 * w + 3]));
+                if (lay == (uint32_t)(CMAX | (CMAX << 8) | (CMAX << 16)))
+                    process_check<CMAX, RW, SAT, false>(a, smem, stage, tb, lay, j, ps0, ps1, absent, cur, dst,
+                                                        trial);
+                else
+                    process_check<CMAX, RW, SAT, true>(a, smem, stage, tb, lay, j, ps0, ps1, absent, cur, dst,
+                                                       trial);
             }
-            if (s_conf[s]) {
+            if (t.conf[s]) {
+                // owner items: APP of the shared group = owner value + guest deltas
                 __syncthreads();
-                if (work) {
-#pragma unroll
-                    for (int e = 0; e < CMAX; e++) {
-                        const uint32_t w = ci[e];
-                        if (e < cnt && ((w >> 25) & 3) == kRoleOwner) {
-                            const int k0 = (w >> 27) & 7, ng = (int)(w >> 30) + 1;
-                            int m = j - (int)((w >> 16) & 0x1ff);
-                            m += (m >> 31) & kM;
-                            int sum = dd[2 + e];
-                            for (int g = 0; g < ng; g++)
-                                sum += stage[(k0 + g) * kM + m];
-                            app[(int)(w & 0xffff) + m] = (int16_t)(SAT ? sat16(sum) : sum);
-                        }
+                if (active) {
+                    const int o0 = t.own_off[s], o1 = t.own_off[s + 1];
+                    for (int k = o0 + lane; k < o1; k += LANES) {
+                        const uint2 it = t.own[k];
+                        const int g0 = (it.y >> 8) & 0xff, ng = (int)(it.y >> 16);
+                        int sum = stage[(int)(it.y & 0xff) * kM + j];
+                        for (int g = 0; g < ng; g++)
+                            sum += stage[(g0 + g) * kM + j];
+                        sts16(smem, (int)it.x + 2 * j, SAT ? sat16(sum) : sum);
                     }
                 }
             }
@@ -306,7 +342,7 @@ __device__ void decode_frame(const DecodeArgs& a, int16_t* app, int16_t* stage, 
                 cur[w] = nxt[w];
         }
     }
-    pack_hard(app, K, a.hard + (size_t)f * (K / 8));
+    pack_hard(reinterpret_cast<const int16_t*>(smem), K, a.hard + (size_t)f * (K / 8));
     if (threadIdx.x == 0)
         a.trials[f] = result;
 }
@@ -399,26 +435,33 @@ __global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc
 {
     extern __shared__ __align__(16) unsigned char smem[];
     int16_t* app = reinterpret_cast<int16_t*>(smem);
-    int16_t* stage = reinterpret_cast<int16_t*>(smem + a.sm_stage);
-    uint32_t* s_circ = reinterpret_cast<uint32_t*>(smem + a.sm_circ);
+    int32_t* stage = reinterpret_cast<int32_t*>(smem + a.sm_stage);
+    uint2* s_tab = reinterpret_cast<uint2*>(smem + a.sm_tab);
     int16_t* s_sched = reinterpret_cast<int16_t*>(smem + a.sm_sched);
-    uint8_t* s_cnt = smem + a.sm_cnt;
+    uint32_t* s_lay = reinterpret_cast<uint32_t*>(smem + a.sm_lay);
     uint8_t* s_conf = smem + a.sm_conf;
+    uint16_t* s_own_off = reinterpret_cast<uint16_t*>(smem + a.sm_own_off);
+    uint2* s_own = reinterpret_cast<uint2*>(smem + a.sm_own);
     float2* pts = reinterpret_cast<float2*>(smem + a.sm_pts);
     int* s_misc = reinterpret_cast<int*>(smem + a.sm_misc);
     const DevCode& c = a.code;
 
     for (int k = threadIdx.x; k < c.q * CMAX; k += blockDim.x)
-        s_circ[k] = c.circ[k];
+        s_tab[k] = c.tab[k];
     for (int k = threadIdx.x; k < 2 * c.n_steps; k += blockDim.x)
         s_sched[k] = c.sched[k];
     for (int k = threadIdx.x; k < c.q; k += blockDim.x)
-        s_cnt[k] = c.cnt[k];
+        s_lay[k] = (uint32_t)c.cnt[k] | ((uint32_t)c.n_plain[k] << 8) | ((uint32_t)c.n_pg[k] << 16);
     for (int k = threadIdx.x; k < c.n_steps; k += blockDim.x)
         s_conf[k] = c.step_conf[k];
+    for (int k = threadIdx.x; k <= c.n_steps; k += blockDim.x)
+        s_own_off[k] = c.own_off[k];
+    for (int k = threadIdx.x; k < c.n_own; k += blockDim.x)
+        s_own[k] = c.own[k];
     if (FUSED && a.dm.kind == 2)
         for (int k = threadIdx.x; k < a.dm.n_points; k += blockDim.x)
             pts[k] = a.dm.points[k];
+    const SmemCode t = {s_tab, s_sched, s_lay, s_conf, s_own_off, s_own};
 
     for (;;) {
         __syncthreads();
@@ -430,9 +473,9 @@ __global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc
             break;
         const int over = FUSED ? demap_into(a, app, pts, f) : load_llr(a, app, f);
         if (__syncthreads_or(over))
-            decode_frame<CMAX, LANES, true>(a, app, stage, s_circ, s_sched, s_cnt, s_conf, f);
+            decode_frame<CMAX, LANES, true>(a, smem, stage, t, f);
         else
-            decode_frame<CMAX, LANES, false>(a, app, stage, s_circ, s_sched, s_cnt, s_conf, f);
+            decode_frame<CMAX, LANES, false>(a, smem, stage, t, f);
     }
 }
 
