@@ -56,10 +56,9 @@ int upload_plan(const cusat::CodePlan& p, DevPlan* d)
 {
     struct Part { const void* src; size_t n; size_t off; };
     Part parts[] = {
-        {p.tab.data(), p.tab.size() * 4, 0},         {p.cnt.data(), p.cnt.size(), 0},
-        {p.n_plain.data(), p.n_plain.size(), 0},     {p.n_pg.data(), p.n_pg.size(), 0},
-        {p.sched.data(), p.sched.size() * 2, 0},     {p.step_conf.data(), p.step_conf.size(), 0},
-        {p.own_off.data(), p.own_off.size() * 2, 0}, {p.own.data(), p.own.size() * 4, 0},
+        {p.tab.data(), p.tab.size() * 4, 0},           {p.sched.data(), p.sched.size() * 2, 0},
+        {p.step_conf.data(), p.step_conf.size(), 0},   {p.item_off.data(), p.item_off.size() * 2, 0},
+        {p.items.data(), p.items.size() * 4, 0},
     };
     size_t total = 0;
     for (auto& pt : parts) {
@@ -82,15 +81,12 @@ int upload_plan(const cusat::CodePlan& p, DevPlan* d)
     c.cmax = p.cmax;
     c.fast_lim = p.fast_lim;
     c.msg_row = p.msg_row;
-    c.n_own = (int)(p.own.size() / 2);
-    c.tab = (const uint2*)(b + parts[0].off);
-    c.cnt = b + parts[1].off;
-    c.n_plain = b + parts[2].off;
-    c.n_pg = b + parts[3].off;
-    c.sched = (const int16_t*)(b + parts[4].off);
-    c.step_conf = b + parts[5].off;
-    c.own_off = (const uint16_t*)(b + parts[6].off);
-    c.own = (const uint2*)(b + parts[7].off);
+    c.n_items = (int)(p.items.size() / 2);
+    c.tab = (const uint4*)(b + parts[0].off);
+    c.sched = (const int16_t*)(b + parts[1].off);
+    c.step_conf = b + parts[2].off;
+    c.item_off = (const uint16_t*)(b + parts[3].off);
+    c.items = (const uint2*)(b + parts[4].off);
     return CUSAT_OK;
 }
 

@@ -7,20 +7,30 @@ namespace cusat {
 
 constexpr int kM = 360;            // circulant size of every DVB-S2/S2X code
 constexpr int kLaneThreads = 384;  // 12 warps per decoding lane (360 check rows)
-constexpr int kMaxStage = 16;      // stage rows (guest deltas + owner values) per step
+constexpr int kMaxStage = 16;      // stage rows per step (one per circulant of a shared group)
 constexpr int kBig = 1 << 20;      // |extrinsic| of an absent edge
 
-// Slot descriptor of one (layer, circulant), uint2:
-//   x = byte offset in the APP of the circulant's first bit (2 * group * 360)
-//   y bits 0-15  r = (360 - shift) mod 360: check j of the layer reads bit
-//                (j + r) mod 360 of the group
-//   y bits 16-23 stage row (guest and owner slots)
-// The circulants of a layer are ordered plain, guest, owner: a plain
-// circulant is the only writer of its bits in the step; when several
-// circulants of one step share an information group, the first is the owner
-// (its updated APP goes to a stage row) and the others are guests (their
-// message deltas go to stage rows); after a barrier the owner items of the
-// step add the rows up.  Owner item, uint2: x = byte offset of the group in
-// the APP, y = owner row | first guest row << 8 | guests << 16.
+// Slot descriptor of one (layer, circulant slot), uint4:
+//   x = byte offset in shared memory of the circulant's first bit
+//   y = r = (360 - shift) mod 360: check j of the layer reads bit
+//       (j + r) mod 360 of the group
+//   z = byte offset from a bit's APP slot to where its update is stored:
+//       0 when the circulant is the only writer of its group in the step;
+//       otherwise the bit's entry in this circulant's stage row
+//   w = kind: 0 plain, 1 staged, 2 absent (the layer has fewer circulants
+//       than the kernel's slots: reads a region of +32767, writes a junk
+//       region, contributes nothing)
+// x and z of staged and absent slots are relative to the stage/dummy
+// regions and are rebased when the kernel copies the table to shared memory,
+// where each descriptor is packed to a uint2 {x, y | z << 9} (z < 2^22).
+// When several circulants of one step share an information group, each
+// writes its updated bits to its own int16 stage row, and a group item of
+// the step (uint2: x = byte offset of the group, y = first row | rows << 8)
+// later stores APP + sum over the rows of (row - APP) (the deltas in the
+// saturating path).  The completion runs at the start of the next step when
+// that step does not touch the group, otherwise after a mid-step barrier.
+constexpr uint32_t kSlotPlain = 0, kSlotStaged = 1, kSlotAbsent = 2;
+constexpr int kStageSets = 2;  // stage rows alternate between even and odd steps
+constexpr uint8_t kConfDefer = 1, kConfMid = 2;
 
 }  // namespace cusat

@@ -12,18 +12,15 @@ namespace cusat {
 struct DevCode {
     int N, K, R, q;
     int n_steps;
-    int cmax;        // circulant slots per layer in the tables (= kernel CMAX)
+    int cmax;        // circulant slots per layer (= kernel CMAX)
     int fast_lim;    // |LLR| bound under which no int16 saturation can occur
     int msg_row;     // bytes of one check row of messages (16 or 32)
-    int n_own;       // owner items over all steps
-    const uint2* tab;          // [q * cmax] slot descriptors (fec_consts.h)
-    const uint8_t* cnt;        // [q] circulants per layer
-    const uint8_t* n_plain;    // [q] plain circulants (first in the layer)
-    const uint8_t* n_pg;       // [q] plain + guest circulants
+    int n_items;     // shared-group items over all steps
+    const uint4* tab;          // [q * cmax] slot descriptors (fec_consts.h)
     const int16_t* sched;      // [n_steps * 2] layer per lane, -1 idle
-    const uint8_t* step_conf;  // [n_steps] 1 if the step has owner items
-    const uint16_t* own_off;   // [n_steps + 1] owner items of step s
-    const uint2* own;          // [n_own]
+    const uint8_t* step_conf;  // [n_steps] 0, kConfDefer or kConfMid
+    const uint16_t* item_off;  // [n_steps + 1] group items of step s
+    const uint2* items;        // [n_items]
 };
 
 // Demapper parameters of one MODCOD (points live in device memory).

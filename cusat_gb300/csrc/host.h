@@ -25,14 +25,12 @@ struct CodePlan {
     int fast_lim = 0;  // |LLR| bound of the saturation-free path
     int max_stage = 0; // stage rows used by the busiest step
     int links_total = 0;
-    std::vector<uint32_t> tab;      // [q * cmax * 2] slot descriptors (fec_consts.h)
-    std::vector<uint8_t> cnt;       // [q]
-    std::vector<uint8_t> n_plain;   // [q]
-    std::vector<uint8_t> n_pg;      // [q]
+    std::vector<uint32_t> tab;      // [q * cmax * 4] slot descriptors (fec_consts.h)
+    std::vector<uint8_t> cnt;       // [q] circulants per layer
     std::vector<int16_t> sched;     // [n_steps * 2]
-    std::vector<uint8_t> step_conf; // [n_steps]
-    std::vector<uint16_t> own_off;  // [n_steps + 1]
-    std::vector<uint32_t> own;      // [n_own * 2] owner items
+    std::vector<uint8_t> step_conf; // [n_steps] 0, kConfDefer or kConfMid
+    std::vector<uint16_t> item_off; // [n_steps + 1]
+    std::vector<uint32_t> items;    // [n_items * 2] shared-group items
     // BCH outer code
     int k_bch = 0, n_bch = 0, t = 0, p = 0;
     uint64_t gen[4] = {0, 0, 0, 0};

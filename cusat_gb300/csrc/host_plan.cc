@@ -114,82 +114,95 @@ void build_plan(CodePlan& c, int framesize, int rate)
         c.lanes = 1;
     }
 
-    // Roles per step: a group (table row) reached by several circulants of
-    // the step has its bits updated by all of them in the same step.  The
-    // first circulant (lane 0 before lane 1, table order) owns the group, the
-    // others are guests; each gets a stage row.  Every layer occurs in exactly
-    // one step, so the role of a circulant is a property of the plan.
-    std::vector<std::vector<int>> role(q);   // per layer, per circulant: 0 plain, 1 guest, 2 owner
-    std::vector<std::vector<int>> srow(q);   // stage row
+    // Shared groups per step: a group (table row) reached by several
+    // circulants of one step has its bits updated by all of them.  Each such
+    // circulant gets its own stage row (rows of one group consecutive, sets
+    // alternating with the step parity); a group item completes the bits.
+    // Every layer occurs in exactly one step, so a slot's staging is a
+    // property of the plan.
+    std::vector<std::vector<int>> srow(q);   // stage row per circulant, -1 = plain
+    std::vector<std::vector<int>> sset(q);
     for (int i = 0; i < q; i++) {
-        role[i].assign(lay[i].size(), 0);
-        srow[i].assign(lay[i].size(), 0);
+        srow[i].assign(lay[i].size(), -1);
+        sset[i].assign(lay[i].size(), 0);
     }
     c.step_conf.assign(c.n_steps, 0);
-    c.own_off.assign(c.n_steps + 1, 0);
-    c.own.clear();
+    c.item_off.assign(c.n_steps + 1, 0);
+    c.items.clear();
     c.max_stage = 0;
+    std::vector<std::vector<int>> shared_groups(c.n_steps);
+    std::vector<std::vector<int>> step_groups(c.n_steps);
     for (int s = 0; s < c.n_steps; s++) {
         struct Ref { int layer, slot, group; };
         std::vector<Ref> refs;
         for (int l = 0; l < 2; l++) {
             const int i = c.sched[2 * s + l];
             if (i >= 0)
-                for (int e = 0; e < (int)lay[i].size(); e++)
+                for (int e = 0; e < (int)lay[i].size(); e++) {
                     refs.push_back({i, e, lay[i][e].first});
+                    step_groups[s].push_back(lay[i][e].first);
+                }
         }
-        std::vector<int> mult(src->n_rows, 0);
+        std::vector<int> mult(src->n_rows, 0), first_row(src->n_rows, -1), used(src->n_rows, 0);
         for (auto& r : refs)
             mult[r.group]++;
         int next_row = 0;
-        std::vector<int> first_ref(src->n_rows, -1);
-        for (int k = 0; k < (int)refs.size(); k++) {
-            const Ref& r = refs[k];
-            if (mult[r.group] < 2 || first_ref[r.group] >= 0)
+        for (auto& r : refs) {
+            if (mult[r.group] < 2)
                 continue;
-            first_ref[r.group] = k;
-            // owner row, then one row per guest, consecutive
-            const int own_row = next_row, g0 = next_row + 1, ng = mult[r.group] - 1;
-            next_row += mult[r.group];
-            role[r.layer][r.slot] = 2;
-            srow[r.layer][r.slot] = own_row;
-            int g = 0;
-            for (int k2 = k + 1; k2 < (int)refs.size(); k2++)
-                if (refs[k2].group == r.group) {
-                    role[refs[k2].layer][refs[k2].slot] = 1;
-                    srow[refs[k2].layer][refs[k2].slot] = g0 + g++;
-                }
-            c.own.push_back((uint32_t)(2 * r.group * kM));
-            c.own.push_back((uint32_t)own_row | ((uint32_t)g0 << 8) | ((uint32_t)ng << 16));
-            c.step_conf[s] = 1;
+            if (first_row[r.group] < 0) {
+                first_row[r.group] = next_row;
+                next_row += mult[r.group];
+                shared_groups[s].push_back(r.group);
+                c.items.push_back((uint32_t)(2 * r.group * kM));
+                c.items.push_back((uint32_t)first_row[r.group] | ((uint32_t)mult[r.group] << 8));
+            }
+            srow[r.layer][r.slot] = first_row[r.group] + used[r.group]++;
+            sset[r.layer][r.slot] = s & 1;
         }
         if (next_row > kMaxStage)
             throw std::runtime_error("step needs more stage rows than the kernel has");
         c.max_stage = std::max(c.max_stage, next_row);
-        c.own_off[s + 1] = (uint16_t)(c.own.size() / 2);
+        c.item_off[s + 1] = (uint16_t)(c.items.size() / 2);
     }
-    // slot descriptors, ordered plain, guest, owner within each layer
-    c.tab.assign((size_t)q * c.cmax * 2, 0);
-    c.n_plain.assign(q, 0);
-    c.n_pg.assign(q, 0);
-    for (int i = 0; i < q; i++) {
-        int slot = 0;
-        for (int want = 0; want < 3; want++) {
-            for (int e = 0; e < (int)lay[i].size(); e++) {
-                if (role[i][e] != want)
-                    continue;
-                const int g = lay[i][e].first, sh = lay[i][e].second;
-                c.tab[((size_t)i * c.cmax + slot) * 2] = (uint32_t)(2 * g * kM);
-                c.tab[((size_t)i * c.cmax + slot) * 2 + 1] =
-                    (uint32_t)((kM - sh) % kM) | ((uint32_t)srow[i][e] << 16);
-                slot++;
+    // completion of a step's shared groups: deferred into the next step when
+    // that step does not touch them, else after a barrier inside the step
+    for (int s = 0; s < c.n_steps; s++) {
+        if (shared_groups[s].empty())
+            continue;
+        bool defer = s + 1 < c.n_steps;
+        if (defer)
+            for (int g : shared_groups[s])
+                for (int g2 : step_groups[s + 1])
+                    if (g == g2)
+                        defer = false;
+        c.step_conf[s] = defer ? kConfDefer : kConfMid;
+    }
+    // slot descriptors
+    c.tab.assign((size_t)q * c.cmax * 4, 0);
+    for (int i = 0; i < q; i++)
+        for (int e = 0; e < c.cmax; e++) {
+            uint32_t* t = &c.tab[((size_t)i * c.cmax + e) * 4];
+            if (e >= (int)lay[i].size()) {
+                t[0] = 0;
+                t[1] = 0;
+                t[2] = (uint32_t)(2 * kM);  // junk region follows the dummy region
+                t[3] = kSlotAbsent;
+                continue;
             }
-            if (want == 0)
-                c.n_plain[i] = (uint8_t)slot;
-            if (want == 1)
-                c.n_pg[i] = (uint8_t)slot;
+            const int g = lay[i][e].first, sh = lay[i][e].second;
+            t[0] = (uint32_t)(2 * g * kM);
+            t[1] = (uint32_t)((kM - sh) % kM);
+            if (srow[i][e] < 0) {
+                t[2] = 0;
+                t[3] = kSlotPlain;
+            } else {
+                // stage entry (relative to the stage region) minus the APP slot
+                const int rel = (sset[i][e] * kMaxStage + srow[i][e]) * 2 * kM;
+                t[2] = (uint32_t)(rel - 2 * g * kM);
+                t[3] = kSlotStaged;
+            }
         }
-    }
 
     // BCH outer code: g = g1 g2 ... gt (reference fec/bch_code.cc:99-122)
     c.k_bch = (int)br->k_bch;

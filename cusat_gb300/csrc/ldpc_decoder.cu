@@ -43,13 +43,14 @@ void decoder_smem_layout(DecodeArgs* a, int cmax, int n_points)
         *field = off;
         off = align16(off + bytes);
     };
-    take(&a->sm_stage, kMaxStage * kM * 4);
+    take(&a->sm_dummy, 2 * kM * 2);  // +32767 region, then the junk region
+    take(&a->sm_stage, kStageSets * kMaxStage * kM * 2);
     take(&a->sm_tab, c.q * cmax * 8);
+    take(&a->sm_cnt, c.q);
     take(&a->sm_sched, c.n_steps * 4);
-    take(&a->sm_lay, c.q * 4);
     take(&a->sm_conf, c.n_steps);
-    take(&a->sm_own_off, (c.n_steps + 1) * 2);
-    take(&a->sm_own, c.n_own * 8);
+    take(&a->sm_item_off, (c.n_steps + 1) * 2);
+    take(&a->sm_items, c.n_items * 8);
     take(&a->sm_pts, n_points * 8);
     take(&a->sm_misc, 16);
     a->sm_total = off;

@@ -29,9 +29,11 @@
 // Checks of one step that share a variable node (a table row with two
 // accumulator addresses in one layer, or in both paired layers) are a data
 // race in the reference (:793-802).  They are resolved deterministically,
-// step-Jacobi: owner and guest circulants (fec_consts.h) write to stage rows
-// instead of the APP, and after a barrier the step's owner items store
-// sat16(APP + all deltas).
+// step-Jacobi: the circulants of a shared group store their updates to
+// their own stage rows instead of the APP (every slot stores to its bit's
+// address plus a per-slot offset, so the body has no per-slot branch), and
+// a group item stores sat16(APP + all deltas) -- at the start of the next
+// step when that step does not touch the group, else after a barrier.
 //
 // Syndrome.  The check before each iteration (reference :693-745) votes
 // after the first step's checks and then every 4 steps, stopping at the
@@ -55,18 +57,17 @@ struct DecodeArgs {
     unsigned int* queue;     // frame counter, zero at launch
     const int16_t* weights;  // learned min-sum weights or nullptr (plain)
     // shared-memory carve-up (bytes)
-    int sm_stage, sm_tab, sm_sched, sm_lay, sm_conf, sm_own_off, sm_own, sm_pts, sm_misc,
-        sm_total;
+    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_misc, sm_total;
 };
 
 // Shared-memory views of the code tables.
 struct SmemCode {
-    const uint2* tab;
+    const uint2* tab;  // per slot: x = bit base, y = r | store offset << 9
+    const uint8_t* cnt;
     const int16_t* sched;
-    const uint32_t* lay;  // per layer: circulants | plain << 8 | plain+guest << 16
     const uint8_t* conf;
-    const uint16_t* own_off;
-    const uint2* own;
+    const uint16_t* item_off;
+    const uint2* items;
 };
 
 __device__ __forceinline__ int sat16(int v) { return max(-32768, min(32767, v)); }
@@ -134,7 +135,6 @@ __device__ bool syndrome_ok(const unsigned char* smem, const SmemCode& t, int K,
                 const int i = t.sched[2 * s + lane];
                 if (i < 0)
                     continue;
-                const int cnt = (int)(t.lay[i] & 0xff);
                 int x = lds16(smem, pty + 2 * (i * kM + j));
                 if (i > 0)
                     x ^= lds16(smem, pty + 2 * ((i - 1) * kM + j));
@@ -142,11 +142,10 @@ __device__ bool syndrome_ok(const unsigned char* smem, const SmemCode& t, int K,
                     x ^= lds16(smem, pty + 2 * ((q - 1) * kM + j - 1));
                 const uint2* tb = t.tab + i * CMAX;
 #pragma unroll
-                for (int e = 0; e < CMAX; e++)
-                    if (e < cnt) {
-                        const uint2 w = tb[e];
-                        x ^= lds16(smem, (int)w.x + 2 * rot360(j, w.y & 0xffff));
-                    }
+                for (int e = 0; e < CMAX; e++) {
+                    const uint2 w = tb[e];
+                    x ^= lds16(smem, (int)w.x + 2 * rot360(j, w.y & 0x1ff));
+                }
                 bad |= x;
             }
         }
@@ -181,22 +180,18 @@ __device__ __forceinline__ int scaled_mag(int r, int beta, int alpha)
 }
 
 // One check row of one layer: gather, offset min-sum, scatter, new message
-// row.  GENERAL handles layers with fewer circulants than CMAX or with
-// owner/guest circulants; the other instantiation is straight-line code for
-// the common layer whose CMAX circulants are all plain.
-template <int CMAX, int RW, bool SAT, bool GENERAL>
-__device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char* smem, int32_t* stage,
-                                              const uint2* tb, uint32_t lay, int j, int ps0, int ps1,
-                                              bool absent, const uint4 (&cur)[RW], uint4* dst, int trial)
+// row; straight-line code for every layer (plain, staged and absent slots
+// differ only in their descriptors).
+template <int CMAX, int RW, bool SAT>
+__device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char* smem, const uint2* tb, int cnt,
+                                              int j, int ps0, int ps1, bool absent, const uint4 (&cur)[RW],
+                                              uint4* dst, int trial)
 {
     constexpr int NE = CMAX + 2;
-    const int cnt = GENERAL ? (int)(lay & 0xff) : CMAX;
-    const int np = GENERAL ? (int)((lay >> 8) & 0xff) : CMAX;
-    const int npg = GENERAL ? (int)((lay >> 16) & 0xff) : CMAX;
     int d[NE];
-    int ad[CMAX];
+    int sa[CMAX];  // where each slot's update is stored (its APP slot, or stage/junk)
     // gather: two parity edges (the second absent for check 0 of layer 0,
-    // which then reads and writes a dummy slot), then the circulants
+    // which then reads and writes a scratch slot), then the circulants
     const int a0 = lds16(smem, ps0);
     const int a1 = lds16(smem, ps1);
     {
@@ -207,15 +202,11 @@ __device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char
     }
 #pragma unroll
     for (int e = 0; e < CMAX; e++) {
-        if (!GENERAL || e < cnt) {
-            const uint2 w = tb[e];
-            ad[e] = (int)w.x + 2 * rot360(j, w.y & 0xffff);
-            const int x = lds16(smem, ad[e]) - row_byte(cur, e + 2);
-            d[2 + e] = SAT ? sat16(x) : x;
-        } else {
-            ad[e] = 0;
-            d[2 + e] = kBig;
-        }
+        const uint2 w = tb[e];
+        const int ad = (int)w.x + 2 * rot360(j, w.y & 0x1ff);
+        sa[e] = ad + ((int)w.y >> 9);
+        const int x = lds16(smem, ad) - row_byte(cur, e + 2);
+        d[2 + e] = SAT ? sat16(x) : x;
     }
     // check node: min1/min2 of |extrinsic|, sign product
     int r1 = kBig, r2 = kBig, sx = 0;
@@ -252,18 +243,18 @@ __device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char
         if (e < 2) {
             // parity: APP = sat16(extrinsic + message)
             sts16(smem, e == 0 ? ps0 : ps1, SAT ? sat16(d[e] + mg) : d[e] + mg);
-        } else if (!GENERAL || e - 2 < cnt) {
-            const int o = e - 2;
-            // SAT: re-read the APP (no other check of the step writes this
-            // bit before the barrier) and saturate once
-            const int nv = SAT ? lds16(smem, ad[o]) + mg - row_byte(cur, e) : d[e] + mg;
-            if (!GENERAL || o < np) {
-                sts16(smem, ad[o], SAT ? sat16(nv) : nv);
+        } else {
+            int v;
+            if (SAT) {
+                // re-read the APP (unchanged: no other check of the step
+                // writes this bit); a staged slot stores its delta, the
+                // completion saturates the sum once
+                const int delta = mg - row_byte(cur, e);
+                v = ((int)tb[e - 2].y >> 9) == 0 ? sat16(lds16(smem, sa[e - 2]) + delta) : delta;
             } else {
-                const uint2 w = tb[o];
-                const int m = (ad[o] - (int)w.x) >> 1;
-                stage[(int)(w.y >> 16) * kM + m] = o < npg ? mg - row_byte(cur, e) : nv;
+                v = d[e] + mg;
             }
+            sts16(smem, sa[e - 2], v);
         }
     }
 #pragma unroll
@@ -271,8 +262,29 @@ __device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char
         __stcg(dst + w, make_uint4(wv[4 * w], wv[4 * w + 1], wv[4 * w + 2], wv[4 * w + 3]));
 }
 
+// Completion of step s's shared groups: thread j of each lane takes bit j of
+// the lane's items.  Plain path: APP + sum(row - APP); saturating path: the
+// rows hold deltas, sat16(APP + sum).
+template <int LANES, bool SAT>
+__device__ __forceinline__ void complete_groups(unsigned char* smem, const int16_t* stage, const SmemCode& t,
+                                                int s, int lane, int j)
+{
+    const int o0 = t.item_off[s], o1 = t.item_off[s + 1];
+    const int16_t* st = stage + (s & 1) * kMaxStage * kM;
+    for (int k = o0 + lane; k < o1; k += LANES) {
+        const uint2 it = t.items[k];
+        const int r0 = (int)(it.y & 0xff), nr = (int)(it.y >> 8);
+        const int app = lds16(smem, (int)it.x + 2 * j);
+        int sum = app;
+        for (int g = 0; g < nr; g++)
+            sum += SAT ? (int)st[(r0 + g) * kM + j] : (int)st[(r0 + g) * kM + j] - app;
+        sts16(smem, (int)it.x + 2 * j, SAT ? sat16(sum) : sum);
+    }
+}
+
 template <int CMAX, int LANES, bool SAT>
-__device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, int32_t* stage, const SmemCode& t, int f)
+__device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, const int16_t* stage, const SmemCode& t,
+                             int f)
 {
     constexpr int NE = CMAX + 2;
     constexpr int RW = (NE + 15) / 16;
@@ -283,7 +295,7 @@ __device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, int32_t* 
     const bool active = j < kM;
     const int K = c.K, q = c.q, T = a.max_trials, n_steps = c.n_steps;
     const int pty = 2 * K;         // byte offset of the parity APP
-    const int dummy = 2 * c.N;     // scratch slot for the absent parity edge
+    const int spare = 2 * c.N;     // scratch slot for the absent parity edge
     uint4* msg_cta = a.msg + (size_t)blockIdx.x * ((size_t)c.R * RW);
     int result = -1;
 
@@ -307,34 +319,22 @@ __device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, int32_t* 
                 const int i_n = s + 1 < n_steps ? t.sched[2 * (s + 1) + lane] : -1;
                 load_row<RW>(nxt, msg_cta + ((size_t)max(i_n, 0) * kM + j) * RW, load && active && i_n >= 0);
             }
-            if (active && i >= 0) {
-                const uint32_t lay = t.lay[i];
-                const int ps0 = pty + 2 * (i * kM + j);
-                const bool absent = (i == 0 && j == 0);
-                const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? dummy : pty + 2 * ((q - 1) * kM + j - 1));
-                const uint2* tb = t.tab + i * CMAX;
-                uint4* dst = msg_cta + ((size_t)i * kM + j) * RW;
-                if (lay == (uint32_t)(CMAX | (CMAX << 8) | (CMAX << 16)))
-                    process_check<CMAX, RW, SAT, false>(a, smem, stage, tb, lay, j, ps0, ps1, absent, cur, dst,
-                                                        trial);
-                else
-                    process_check<CMAX, RW, SAT, true>(a, smem, stage, tb, lay, j, ps0, ps1, absent, cur, dst,
-                                                       trial);
-            }
-            if (t.conf[s]) {
-                // owner items: APP of the shared group = owner value + guest deltas
-                __syncthreads();
-                if (active) {
-                    const int o0 = t.own_off[s], o1 = t.own_off[s + 1];
-                    for (int k = o0 + lane; k < o1; k += LANES) {
-                        const uint2 it = t.own[k];
-                        const int g0 = (it.y >> 8) & 0xff, ng = (int)(it.y >> 16);
-                        int sum = stage[(int)(it.y & 0xff) * kM + j];
-                        for (int g = 0; g < ng; g++)
-                            sum += stage[(g0 + g) * kM + j];
-                        sts16(smem, (int)it.x + 2 * j, SAT ? sat16(sum) : sum);
-                    }
+            if (active) {
+                // groups of the previous step whose completion was deferred
+                if (s > 0 && t.conf[s - 1] == kConfDefer)
+                    complete_groups<LANES, SAT>(smem, stage, t, s - 1, lane, j);
+                if (i >= 0) {
+                    const int ps0 = pty + 2 * (i * kM + j);
+                    const bool absent = (i == 0 && j == 0);
+                    const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? spare : pty + 2 * ((q - 1) * kM + j - 1));
+                    process_check<CMAX, RW, SAT>(a, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent, cur,
+                                                 msg_cta + ((size_t)i * kM + j) * RW, trial);
                 }
+            }
+            if (t.conf[s] == kConfMid) {
+                __syncthreads();
+                if (active)
+                    complete_groups<LANES, SAT>(smem, stage, t, s, lane, j);
             }
             __syncthreads();
 #pragma unroll
@@ -435,33 +435,48 @@ __global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc
 {
     extern __shared__ __align__(16) unsigned char smem[];
     int16_t* app = reinterpret_cast<int16_t*>(smem);
-    int32_t* stage = reinterpret_cast<int32_t*>(smem + a.sm_stage);
+    int16_t* dummy = reinterpret_cast<int16_t*>(smem + a.sm_dummy);
+    const int16_t* stage = reinterpret_cast<const int16_t*>(smem + a.sm_stage);
     uint2* s_tab = reinterpret_cast<uint2*>(smem + a.sm_tab);
+    uint8_t* s_cnt = smem + a.sm_cnt;
     int16_t* s_sched = reinterpret_cast<int16_t*>(smem + a.sm_sched);
-    uint32_t* s_lay = reinterpret_cast<uint32_t*>(smem + a.sm_lay);
     uint8_t* s_conf = smem + a.sm_conf;
-    uint16_t* s_own_off = reinterpret_cast<uint16_t*>(smem + a.sm_own_off);
-    uint2* s_own = reinterpret_cast<uint2*>(smem + a.sm_own);
+    uint16_t* s_item_off = reinterpret_cast<uint16_t*>(smem + a.sm_item_off);
+    uint2* s_items = reinterpret_cast<uint2*>(smem + a.sm_items);
     float2* pts = reinterpret_cast<float2*>(smem + a.sm_pts);
     int* s_misc = reinterpret_cast<int*>(smem + a.sm_misc);
     const DevCode& c = a.code;
 
-    for (int k = threadIdx.x; k < c.q * CMAX; k += blockDim.x)
-        s_tab[k] = c.tab[k];
+    // slot descriptors, rebased onto this kernel's stage and dummy regions
+    // and packed to 8 bytes: x = bit base, y = r | store offset << 9
+    for (int k = threadIdx.x; k < c.q * CMAX; k += blockDim.x) {
+        uint4 w = c.tab[k];
+        if (w.w == kSlotStaged)
+            w.z += (uint32_t)a.sm_stage;
+        else if (w.w == kSlotAbsent)
+            w.x = (uint32_t)a.sm_dummy;
+        s_tab[k] = make_uint2(w.x, w.y | (w.z << 9));
+    }
+    for (int k = threadIdx.x; k < c.q; k += blockDim.x) {
+        int n = 0;
+        for (int e = 0; e < CMAX; e++)
+            n += c.tab[k * CMAX + e].w != kSlotAbsent;
+        s_cnt[k] = (uint8_t)n;
+    }
+    for (int k = threadIdx.x; k < kM; k += blockDim.x)
+        dummy[k] = 32767;  // absent circulants read +32767: never a minimum, no sign
     for (int k = threadIdx.x; k < 2 * c.n_steps; k += blockDim.x)
         s_sched[k] = c.sched[k];
-    for (int k = threadIdx.x; k < c.q; k += blockDim.x)
-        s_lay[k] = (uint32_t)c.cnt[k] | ((uint32_t)c.n_plain[k] << 8) | ((uint32_t)c.n_pg[k] << 16);
     for (int k = threadIdx.x; k < c.n_steps; k += blockDim.x)
         s_conf[k] = c.step_conf[k];
     for (int k = threadIdx.x; k <= c.n_steps; k += blockDim.x)
-        s_own_off[k] = c.own_off[k];
-    for (int k = threadIdx.x; k < c.n_own; k += blockDim.x)
-        s_own[k] = c.own[k];
+        s_item_off[k] = c.item_off[k];
+    for (int k = threadIdx.x; k < c.n_items; k += blockDim.x)
+        s_items[k] = c.items[k];
     if (FUSED && a.dm.kind == 2)
         for (int k = threadIdx.x; k < a.dm.n_points; k += blockDim.x)
             pts[k] = a.dm.points[k];
-    const SmemCode t = {s_tab, s_sched, s_lay, s_conf, s_own_off, s_own};
+    const SmemCode t = {s_tab, s_cnt, s_sched, s_conf, s_item_off, s_items};
 
     for (;;) {
         __syncthreads();
