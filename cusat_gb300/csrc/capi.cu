@@ -230,6 +230,10 @@ struct DevDemapObj {
 
 }  // namespace
 
+namespace cusat {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace cusat
+
 struct cusat_ldpc_decoder {
     Engine eng;
     int16_t* soft_dev = nullptr;

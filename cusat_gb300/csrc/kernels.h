@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "fec_device.cuh"
 
 namespace cusat {
@@ -34,6 +36,9 @@ int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, c
 
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream);
+// Sets the message returned by cusat_last_error() on this thread.
+void set_last_error(const std::string& msg);
+
 int launch_bch_check(const BchDev& t, const uint8_t* cw, int32_t* valid, uint8_t* rem, int batch,
                      cudaStream_t stream);
 

@@ -171,6 +171,29 @@ int cusat_rx_fec_launch(cusat_rx_fec* rx, const float* sym_dev, int batch, float
                         int32_t* bch_valid_out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Decoding without device allocation                                      */
+/* ---------------------------------------------------------------------- */
+
+/* No counterpart in the reference.  For callers that may not allocate
+ * device memory (a real-time thread under a no-allocation rule, a host
+ * application whose memory pool owns every device allocation): decodes like
+ * cusat_ldpc_decode_launch -- same kernel,
+ * same results -- but every buffer besides the caller's LLRs (soft_dev,
+ * batch * n_ldpc int16, device) and outputs (hard_out batch * k_ldpc/8
+ * bytes, trials_out batch int32, device or mapped pinned) is a fixed array
+ * inside the library: 24 MiB of message rows (which bounds the CTAs used:
+ * 60 for normal rate 3/5), 64 KiB of code tables, a frame counter.  They
+ * exist on every device that loads the library until the process exits.
+ * The first call on a device looks up their addresses and must come before
+ * any stream capture; a call whose code differs from the previous call's
+ * copies the new code's tables from host memory.  All calls on a device
+ * share its arrays: calls whose kernels overlap on the GPU race.  Returns
+ * CUSAT_ERR_ARG when a code's tables or one frame's message rows exceed the
+ * arrays (no DVB-S2/S2X code does). */
+int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int16_t* soft_dev, int batch,
+                              uint8_t* hard_out, int32_t* trials_out, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Code description and traffic generation (host side; used to generate     */
 /* test and benchmark traffic, not part of the receive path)               */
 /* ---------------------------------------------------------------------- */
