@@ -27,7 +27,7 @@ from ._capi import CusatError
 from .enums import *  # noqa: F401,F403
 from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
 
-__all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec",
+__all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch",
            "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
            "CusatError", "library_path"]
 
@@ -318,3 +318,60 @@ class rx_fec:
         _capi.check(_capi.lib().cusat_rx_fec_launch(self._h, _addr(sym_dev), batch_size, noise_var, llr_gain,
                                                     _addr(hard_out), _addr(trials_out), _addr(bch_valid_out),
                                                     _stream(stream)))
+
+
+class batch:
+    """Mixed-MODCOD batch decoder: frames of any of `modcods` ((modulation,
+    rate, frame size) triples) in one launch sequence (fused demap -> decode
+    -> BCH), optionally captured into a CUDA graph.  No counterpart in the
+    reference (one chain per MODCOD, lib/cusat_dsp/rx_fec_pool.cc:48-87)."""
+
+    def __init__(self, modcods, max_trials=50, max_frames=1024):
+        arr = np.ascontiguousarray(np.asarray(modcods, np.int32).reshape(-1, 3))
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_batch_create(arr.ctypes.data, arr.shape[0], max_trials, max_frames,
+                                                   ctypes.byref(h)))
+        self._h = h
+        self.modcods = [tuple(int(v) for v in r) for r in arr]
+        self.max_trials, self.max_frames = max_trials, max_frames
+        self._frames = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def info(self):
+        return _info(_capi.lib().cusat_batch_info, self._h, 4)
+
+    @staticmethod
+    def frames(modcod, noise_var, llr_gain, sym, hard, trials, bch_valid=None):
+        """Array of cusat_frame from per-frame lists (addresses or tensors)."""
+        n = len(modcod)
+        arr = (_capi.Frame * n)()
+        for i in range(n):
+            arr[i] = _capi.Frame(int(modcod[i]), float(noise_var[i]), float(llr_gain[i]), 0, _addr(sym[i]),
+                                 _addr(hard[i]), _addr(trials[i]),
+                                 None if bch_valid is None else _addr(bch_valid[i]))
+        return arr
+
+    def launch(self, frames, stream=None):
+        self._frames = frames
+        _capi.check(_capi.lib().cusat_batch_launch(self._h, ctypes.addressof(frames), len(frames),
+                                                   _stream(stream)))
+
+    def tune(self, frames, reps=3, stream=None):
+        best = ctypes.c_float()
+        _capi.check(_capi.lib().cusat_batch_tune(self._h, ctypes.addressof(frames), len(frames), reps,
+                                                 _stream(stream), ctypes.byref(best)))
+        return best.value
+
+    def capture(self, frames, stream):
+        self._frames = frames
+        _capi.check(_capi.lib().cusat_batch_capture(self._h, ctypes.addressof(frames), len(frames),
+                                                    _stream(stream)))
+
+    def replay(self, stream):
+        _capi.check(_capi.lib().cusat_batch_replay(self._h, _stream(stream)))

@@ -58,6 +58,15 @@ _SIGS = {
                                            ctypes.c_void_p]),
     "cusat_ldpc_decode_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "cusat_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_batch_destroy": (None, [ctypes.c_void_p]),
+    "cusat_batch_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "cusat_batch_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
+    "cusat_batch_capture": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "cusat_batch_replay": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "cusat_code_info": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_int_p]),
     "cusat_gen_encode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int]),
@@ -68,6 +77,13 @@ _SIGS = {
     "cusat_modcod_capped_llr_gain": (ctypes.c_float, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                       ctypes.c_float]),
 }
+
+
+class Frame(ctypes.Structure):
+    """cusat_frame of include/cusat_fec.h."""
+    _fields_ = [("modcod", ctypes.c_int32), ("noise_var", ctypes.c_float), ("llr_gain", ctypes.c_float),
+                ("reserved", ctypes.c_int32), ("sym", ctypes.c_void_p), ("hard", ctypes.c_void_p),
+                ("trials", ctypes.c_void_p), ("bch_valid", ctypes.c_void_p)]
 
 
 class CusatError(RuntimeError):

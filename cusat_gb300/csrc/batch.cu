@@ -1,0 +1,472 @@
+// Mixed-MODCOD batches: one launch decodes frames of many MODCODs and frame
+// sizes (symbols in; hard decisions, iteration counts, BCH flags out).
+//
+// The MODCODs of a batch fall into kernel classes (circulant slots per layer
+// x lanes); each class runs one persistent decoder kernel over its frames,
+// reloading a code's tables into shared memory when consecutive frames of a
+// CTA change code.  The class kernels run concurrently on forked streams and
+// one mixed-code BCH kernel follows; the whole sequence can be captured once
+// into a CUDA graph and replayed.  A measurement-driven tuner picks each
+// class's grid (number of persistent CTAs) and the class launch order.
+// The reference decodes one MODCOD per chain and launches per
+// (chain, micro-batch, stream) (lib/cusat_dsp/rx_fec_chain.cc:361-505,
+// rx_fec_pool.cc:48-87).
+#include <algorithm>
+#include <map>
+#include <memory>
+
+#include "engine.h"
+
+using namespace cusat_internal;
+
+namespace {
+
+struct ModcodObj {
+    int mod = 0, rate = 0, fs = 0;
+    const cusat::CodePlan* plan = nullptr;
+    DevPlan dp;
+    DevDemapObj dm;
+    DevBch bch;
+    int cls = -1;       // kernel class
+    int code_in_class = 0;
+};
+
+struct KernelClass {
+    int cmax = 0, lanes = 0;
+    const void* fn = nullptr;
+    int threads = 0, per_sm = 0, grid_max = 0;
+    cusat::DecodeArgs proto{};
+    std::vector<int> modcods;  // modcod indices, position = code index in the class
+    cusat::DevCode* d_codes = nullptr;
+    cusat::DevDemap* d_demaps = nullptr;
+    cusat::FrameDesc* d_frames = nullptr;
+    uint4* msg = nullptr;
+    unsigned int* queue = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    // tuned launch: fraction of grid_max (1.0 = every resident CTA slot)
+    float grid_frac = 1.0f;
+};
+
+}  // namespace
+
+struct cusat_batch {
+    std::vector<std::unique_ptr<ModcodObj>> modcods;
+    std::vector<KernelClass> classes;
+    std::vector<int> order;  // class launch order
+    int max_trials = 0, max_frames = 0, sms = 0;
+    // staging (pinned) and device descriptors
+    cusat::FrameDesc* h_frames = nullptr;   // [max_frames], grouped by class
+    cusat::BchFrame* h_bch = nullptr;       // [max_frames]
+    cusat::FrameDesc* d_frames = nullptr;
+    cusat::BchFrame* d_bch = nullptr;
+    cusat::BchDev* d_bch_codes = nullptr;
+    std::vector<int> class_count, class_off;
+    cudaEvent_t fork = nullptr;
+    // captured sequence: its own device descriptors (written once at capture),
+    // so that later launches with other frames leave it intact
+    cudaGraphExec_t graph = nullptr;
+    cusat::FrameDesc* g_frames = nullptr;
+    cusat::BchFrame* g_bch = nullptr;
+    int graph_frames = 0;
+};
+
+namespace {
+
+void release(cusat_batch* b)
+{
+    if (!b)
+        return;
+    if (b->graph)
+        cudaGraphExecDestroy(b->graph);
+    for (auto& c : b->classes) {
+        if (c.d_codes) cudaFree(c.d_codes);
+        if (c.d_demaps) cudaFree(c.d_demaps);
+        if (c.msg) cudaFree(c.msg);
+        if (c.queue) cudaFree(c.queue);
+        if (c.stream) cudaStreamDestroy(c.stream);
+        if (c.done) cudaEventDestroy(c.done);
+    }
+    for (auto& m : b->modcods) {
+        m->dp.blob ? (void)cudaFree(m->dp.blob) : (void)0;
+        m->dm.release();
+        m->bch.release();
+    }
+    if (b->h_frames) cudaFreeHost(b->h_frames);
+    if (b->h_bch) cudaFreeHost(b->h_bch);
+    if (b->d_frames) cudaFree(b->d_frames);
+    if (b->d_bch) cudaFree(b->d_bch);
+    if (b->d_bch_codes) cudaFree(b->d_bch_codes);
+    if (b->g_frames) cudaFree(b->g_frames);
+    if (b->g_bch) cudaFree(b->g_bch);
+    if (b->fork) cudaEventDestroy(b->fork);
+    delete b;
+}
+
+// Writes the staged descriptors of frames[0..n) grouped by class.
+int stage(cusat_batch* b, const cusat_frame* frames, int n)
+{
+    const int nc = (int)b->classes.size();
+    b->class_count.assign(nc, 0);
+    for (int i = 0; i < n; i++) {
+        const int m = frames[i].modcod;
+        if (m < 0 || m >= (int)b->modcods.size())
+            return fail(CUSAT_ERR_ARG, "frame refers to an unknown MODCOD index");
+        if (!frames[i].sym || !frames[i].hard || !frames[i].trials)
+            return fail(CUSAT_ERR_ARG, "null frame buffer");
+        b->class_count[b->modcods[m]->cls]++;
+    }
+    b->class_off.assign(nc + 1, 0);
+    for (int k = 0; k < nc; k++)
+        b->class_off[k + 1] = b->class_off[k] + b->class_count[k];
+    // within a class, frames ordered by code so that CTAs rarely reload tables
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++)
+        idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+        const ModcodObj& a = *b->modcods[frames[x].modcod];
+        const ModcodObj& c = *b->modcods[frames[y].modcod];
+        return a.cls != c.cls ? a.cls < c.cls : a.code_in_class < c.code_in_class;
+    });
+    for (int k = 0; k < n; k++) {
+        const cusat_frame& fr = frames[idx[k]];
+        const ModcodObj& m = *b->modcods[fr.modcod];
+        cusat::FrameDesc& d = b->h_frames[k];
+        d.code = m.code_in_class;
+        d.noise_var = fr.noise_var;
+        d.llr_gain = cusat::capped_llr_gain(m.dm.m, fr.llr_gain);
+        d.pad = 0;
+        d.in = fr.sym;
+        d.hard = fr.hard;
+        d.trials = fr.trials;
+        cusat::BchFrame& c = b->h_bch[k];
+        c.code = fr.modcod;
+        c.pad = 0;
+        c.cw = fr.hard;
+        c.valid = fr.bch_valid;
+    }
+    return CUSAT_OK;
+}
+
+// Launch sequence for n staged frames whose descriptors are (or, with
+// `copy`, are first copied from the pinned staging arrays) at d_frames/d_bch.
+int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, cusat::BchFrame* d_bch, bool copy)
+{
+    if (copy) {
+        CU(cudaMemcpyAsync(d_frames, b->h_frames, (size_t)n * sizeof(cusat::FrameDesc), cudaMemcpyHostToDevice, s),
+           "cudaMemcpyAsync(frames)");
+        CU(cudaMemcpyAsync(d_bch, b->h_bch, (size_t)n * sizeof(cusat::BchFrame), cudaMemcpyHostToDevice, s),
+           "cudaMemcpyAsync(bch frames)");
+    }
+    CU(cudaEventRecord(b->fork, s), "cudaEventRecord");
+    for (int k : b->order) {
+        KernelClass& c = b->classes[k];
+        const int cnt = b->class_count[k];
+        if (!cnt)
+            continue;
+        CU(cudaStreamWaitEvent(c.stream, b->fork, 0), "cudaStreamWaitEvent");
+        CU(cudaMemsetAsync(c.queue, 0, sizeof(unsigned int), c.stream), "cudaMemsetAsync(queue)");
+        cusat::DecodeArgs a = c.proto;
+        a.frames = d_frames + b->class_off[k];
+        a.n_frames = cnt;
+        int grid = std::max(1, (int)(c.grid_frac * c.grid_max + 0.5f));
+        grid = std::min(grid, std::min(cnt, c.grid_max));
+        const int rc = cusat::launch_decoder(c.fn, a, grid, c.threads, c.stream);
+        if (rc)
+            return cuda_fail((cudaError_t)rc, "decoder launch");
+        CU(cudaEventRecord(c.done, c.stream), "cudaEventRecord");
+        CU(cudaStreamWaitEvent(s, c.done, 0), "cudaStreamWaitEvent");
+    }
+    const int rc = cusat::launch_bch_check_mixed(b->d_bch_codes, d_bch, n, s);
+    if (rc)
+        return cuda_fail((cudaError_t)rc, "BCH launch");
+    return CUSAT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, int max_frames, cusat_batch** out)
+{
+    if (!out || !modcods || n_modcods <= 0 || n_modcods > 256 || max_frames <= 0 || max_trials < 0 ||
+        max_trials > 1000)
+        return fail(CUSAT_ERR_ARG, "invalid batch arguments");
+    *out = nullptr;
+    int dev;
+    int rc = require_device(&dev);
+    if (rc)
+        return rc;
+    cusat_batch* b = new cusat_batch();
+    b->max_trials = max_trials;
+    b->max_frames = max_frames;
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    std::map<std::pair<int, int>, int> class_of;
+    for (int i = 0; i < n_modcods && rc == CUSAT_OK; i++) {
+        auto m = std::make_unique<ModcodObj>();
+        m->mod = modcods[3 * i];
+        m->rate = modcods[3 * i + 1];
+        m->fs = modcods[3 * i + 2];
+        std::string err;
+        m->plan = cusat::get_code_plan(m->fs, m->rate, &err);
+        if (!m->plan) {
+            rc = fail(CUSAT_ERR_UNSUPPORTED, err);
+            break;
+        }
+        rc = upload_plan(*m->plan, &m->dp);
+        if (rc == CUSAT_OK)
+            rc = m->dm.init(m->mod, m->rate, m->fs);
+        if (rc == CUSAT_OK && m->dm.m.interleaved_len != m->dm.m.xfec)
+            rc = fail(CUSAT_ERR_UNSUPPORTED, "padded XFECFRAME");
+        if (rc == CUSAT_OK)
+            rc = m->bch.init(m->plan->gen, m->plan->p, (unsigned)(m->plan->n_bch / 8));
+        if (rc)
+            break;
+        const auto key = std::make_pair(m->plan->cmax, m->plan->lanes);
+        if (!class_of.count(key)) {
+            class_of[key] = (int)b->classes.size();
+            KernelClass c;
+            c.cmax = key.first;
+            c.lanes = key.second;
+            b->classes.push_back(c);
+        }
+        m->cls = class_of[key];
+        m->code_in_class = (int)b->classes[m->cls].modcods.size();
+        b->classes[m->cls].modcods.push_back(i);
+        b->modcods.push_back(std::move(m));
+    }
+    // per class: kernel, shared-memory layout for its largest code, tables,
+    // message scratch for every resident CTA, stream
+    for (size_t k = 0; k < b->classes.size() && rc == CUSAT_OK; k++) {
+        KernelClass& c = b->classes[k];
+        cusat::SmemDims dims{0, 0, 0, 0, c.cmax, 0};
+        size_t msg_cta = 0;
+        std::vector<cusat::DevCode> codes;
+        std::vector<cusat::DevDemap> demaps;
+        for (int mi : c.modcods) {
+            const ModcodObj& m = *b->modcods[mi];
+            const cusat::DevCode& dc = m.dp.code;
+            dims.N = std::max(dims.N, dc.N);
+            dims.q = std::max(dims.q, dc.q);
+            dims.n_steps = std::max(dims.n_steps, dc.n_steps);
+            dims.n_items = std::max(dims.n_items, dc.n_items);
+            dims.n_points = std::max(dims.n_points, m.dm.m.kind == 2 ? m.dm.m.n_points : 0);
+            msg_cta = std::max(msg_cta, (size_t)dc.R * dc.msg_row);
+            codes.push_back(dc);
+            demaps.push_back(m.dm.d);
+        }
+        c.fn = cusat::select_decoder_kernel(c.cmax, c.lanes, true);
+        c.threads = cusat::decoder_threads(c.lanes);
+        memset(&c.proto, 0, sizeof(c.proto));
+        c.proto.max_trials = max_trials;
+        cusat::decoder_smem_layout(&c.proto, dims);
+        if (!c.fn || c.proto.sm_total > optin) {
+            rc = fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel fits this MODCOD");
+            break;
+        }
+        cudaError_t e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, c.proto.sm_total);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sm, c.fn, c.threads, c.proto.sm_total);
+        c.grid_max = c.per_sm * b->sms;
+        if (e == cudaSuccess)
+            e = cudaMalloc(&c.d_codes, codes.size() * sizeof(cusat::DevCode));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(c.d_codes, codes.data(), codes.size() * sizeof(cusat::DevCode), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&c.d_demaps, demaps.size() * sizeof(cusat::DevDemap));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(c.d_demaps, demaps.data(), demaps.size() * sizeof(cusat::DevDemap),
+                           cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&c.msg, (size_t)c.grid_max * msg_cta);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&c.queue, 256);
+        if (e == cudaSuccess)
+            e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "batch class set-up");
+            break;
+        }
+        c.proto.codes = c.d_codes;
+        c.proto.demaps = c.d_demaps;
+        c.proto.msg = c.msg;
+        c.proto.msg_stride = (int)(msg_cta / 16);
+        c.proto.queue = c.queue;
+        b->order.push_back((int)k);
+    }
+    if (rc == CUSAT_OK) {
+        std::vector<cusat::BchDev> bch;
+        for (auto& m : b->modcods)
+            bch.push_back(m->bch.d);
+        cudaError_t e = cudaMallocHost(&b->h_frames, (size_t)max_frames * sizeof(cusat::FrameDesc));
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&b->h_bch, (size_t)max_frames * sizeof(cusat::BchFrame));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&b->d_frames, (size_t)max_frames * sizeof(cusat::FrameDesc));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&b->d_bch, (size_t)max_frames * sizeof(cusat::BchFrame));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&b->d_bch_codes, bch.size() * sizeof(cusat::BchDev));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_bch_codes, bch.data(), bch.size() * sizeof(cusat::BchDev), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "batch buffers");
+    }
+    if (rc != CUSAT_OK) {
+        release(b);
+        return rc;
+    }
+    *out = b;
+    return CUSAT_OK;
+}
+
+void cusat_batch_destroy(cusat_batch* b) { release(b); }
+
+int cusat_batch_info(const cusat_batch* b, int32_t* out)
+{
+    if (!b || !out)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    out[0] = (int32_t)b->modcods.size();
+    out[1] = (int32_t)b->classes.size();
+    out[2] = b->max_frames;
+    out[3] = b->max_trials;
+    return CUSAT_OK;
+}
+
+int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* stream)
+{
+    if (!b || !frames || n <= 0 || n > b->max_frames)
+        return fail(CUSAT_ERR_ARG, "frames outside 1..max_frames");
+    // the staging buffers are read by the copies of the previous launch
+    CU(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+    int rc = stage(b, frames, n);
+    if (rc)
+        return rc;
+    return enqueue(b, n, (cudaStream_t)stream, b->d_frames, b->d_bch, true);
+}
+
+int cusat_batch_capture(cusat_batch* b, const cusat_frame* frames, int n, void* stream)
+{
+    if (!b || !frames || n <= 0 || n > b->max_frames)
+        return fail(CUSAT_ERR_ARG, "frames outside 1..max_frames");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!s)
+        return fail(CUSAT_ERR_ARG, "graph capture needs a created stream");
+    CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    int rc = stage(b, frames, n);
+    if (rc)
+        return rc;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    if (!b->g_frames) {
+        CU(cudaMalloc(&b->g_frames, (size_t)b->max_frames * sizeof(cusat::FrameDesc)), "cudaMalloc(graph frames)");
+        CU(cudaMalloc(&b->g_bch, (size_t)b->max_frames * sizeof(cusat::BchFrame)), "cudaMalloc(graph frames)");
+    }
+    CU(cudaMemcpy(b->g_frames, b->h_frames, (size_t)n * sizeof(cusat::FrameDesc), cudaMemcpyHostToDevice),
+       "cudaMemcpy(graph frames)");
+    CU(cudaMemcpy(b->g_bch, b->h_bch, (size_t)n * sizeof(cusat::BchFrame), cudaMemcpyHostToDevice),
+       "cudaMemcpy(graph frames)");
+    CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    rc = enqueue(b, n, s, b->g_frames, b->g_bch, false);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc)
+        return rc;
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaStreamEndCapture");
+    const cudaError_t e2 = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess)
+        return cuda_fail(e2, "cudaGraphInstantiate");
+    b->graph_frames = n;
+    return CUSAT_OK;
+}
+
+int cusat_batch_replay(cusat_batch* b, void* stream)
+{
+    if (!b || !b->graph)
+        return fail(CUSAT_ERR_ARG, "no captured batch");
+    CU(cudaGraphLaunch(b->graph, (cudaStream_t)stream), "cudaGraphLaunch");
+    return CUSAT_OK;
+}
+
+int cusat_batch_tune(cusat_batch* b, const cusat_frame* frames, int n, int reps, void* stream, float* best_ms)
+{
+    if (!b || !frames || n <= 0 || n > b->max_frames || reps <= 0)
+        return fail(CUSAT_ERR_ARG, "invalid tuning arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    int rc = stage(b, frames, n);
+    if (rc)
+        return rc;
+    const int nc = (int)b->classes.size();
+    // work of a class ~ frames x edges; classes with more work launch first
+    std::vector<double> work(nc, 0.0);
+    for (int i = 0; i < n; i++) {
+        const ModcodObj& m = *b->modcods[frames[i].modcod];
+        work[m.cls] += m.plan->links_total;
+    }
+    double total = 0;
+    for (double w : work)
+        total += w;
+    std::vector<int> by_work(nc);
+    for (int k = 0; k < nc; k++)
+        by_work[k] = k;
+    std::sort(by_work.begin(), by_work.end(), [&](int x, int y) { return work[x] > work[y]; });
+    std::vector<int> by_work_rev(by_work.rbegin(), by_work.rend());
+    // candidates: (order, grid rule); grid rule 0 = every resident slot,
+    // 1 = slots in proportion to the class's share of the work
+    struct Cand { const std::vector<int>* order; int rule; };
+    const Cand cands[] = {{&by_work, 0}, {&by_work, 1}, {&by_work_rev, 0}, {&by_work_rev, 1}};
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0), "cudaEventCreate");
+    CU(cudaEventCreate(&e1), "cudaEventCreate");
+    float best = 1e30f;
+    int best_i = 0;
+    for (int ci = 0; ci < 4; ci++) {
+        b->order = *cands[ci].order;
+        for (int k = 0; k < nc; k++)
+            b->classes[k].grid_frac =
+                cands[ci].rule == 0 ? 1.0f : (float)std::max(0.05, total > 0 ? work[k] / total : 1.0);
+        float sum = 0;
+        for (int r = 0; r <= reps; r++) {
+            CU(cudaEventRecord(e0, s), "cudaEventRecord");
+            rc = enqueue(b, n, s, b->d_frames, b->d_bch, true);
+            if (rc)
+                break;
+            CU(cudaEventRecord(e1, s), "cudaEventRecord");
+            CU(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0)
+                sum += ms;  // first run warms the caches and the instruction cache
+        }
+        if (rc)
+            break;
+        if (sum / reps < best) {
+            best = sum / reps;
+            best_i = ci;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc)
+        return rc;
+    b->order = *cands[best_i].order;
+    for (int k = 0; k < nc; k++)
+        b->classes[k].grid_frac =
+            cands[best_i].rule == 0 ? 1.0f : (float)std::max(0.05, total > 0 ? work[k] / total : 1.0);
+    if (best_ms)
+        *best_ms = best;
+    return CUSAT_OK;
+}
+
+}  // extern "C"

@@ -7,88 +7,21 @@
 #include <vector>
 
 #include "../../include/cusat_fec.h"
-#include "host.h"
-#include "kernels.h"
-#include "ldpc_kernel.cuh"
+#include "engine.h"
 
 namespace {
 
 thread_local std::string g_last_error;
 
-int fail(int code, const std::string& msg)
-{
-    g_last_error = msg;
-    return code;
-}
+}  // namespace
 
-int cuda_fail(cudaError_t e, const char* what)
-{
-    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
-    return CUSAT_ERR_CUDA;
-}
+namespace cusat {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace cusat
 
-#define CU(call, what)                          \
-    do {                                        \
-        cudaError_t e_ = (call);                \
-        if (e_ != cudaSuccess)                  \
-            return cuda_fail(e_, what);         \
-    } while (0)
+using namespace cusat_internal;
 
-int require_device(int* dev)
-{
-    int n = 0;
-    cudaError_t e = cudaGetDeviceCount(&n);
-    if (e != cudaSuccess || n == 0)
-        return fail(CUSAT_ERR_NO_DEVICE, "no CUDA device");
-    e = cudaGetDevice(dev);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "cudaGetDevice");
-    return CUSAT_OK;
-}
-
-// Device copy of a code plan (one allocation).
-struct DevPlan {
-    void* blob = nullptr;
-    cusat::DevCode code{};
-};
-
-int upload_plan(const cusat::CodePlan& p, DevPlan* d)
-{
-    struct Part { const void* src; size_t n; size_t off; };
-    Part parts[] = {
-        {p.tab.data(), p.tab.size() * 4, 0},           {p.sched.data(), p.sched.size() * 2, 0},
-        {p.step_conf.data(), p.step_conf.size(), 0},   {p.item_off.data(), p.item_off.size() * 2, 0},
-        {p.items.data(), p.items.size() * 4, 0},
-    };
-    size_t total = 0;
-    for (auto& pt : parts) {
-        pt.off = total;
-        total += (pt.n + 255) & ~(size_t)255;
-    }
-    std::vector<unsigned char> h(total + 256, 0);
-    for (auto& pt : parts)
-        if (pt.n)
-            memcpy(&h[pt.off], pt.src, pt.n);
-    CU(cudaMalloc(&d->blob, total + 256), "cudaMalloc(plan)");
-    CU(cudaMemcpy(d->blob, h.data(), total + 256, cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
-    unsigned char* b = (unsigned char*)d->blob;
-    cusat::DevCode& c = d->code;
-    c.N = p.N;
-    c.K = p.K;
-    c.R = p.R;
-    c.q = p.q;
-    c.n_steps = p.n_steps;
-    c.cmax = p.cmax;
-    c.fast_lim = p.fast_lim;
-    c.msg_row = p.msg_row;
-    c.n_items = (int)(p.items.size() / 2);
-    c.tab = (const uint4*)(b + parts[0].off);
-    c.sched = (const int16_t*)(b + parts[1].off);
-    c.step_conf = b + parts[2].off;
-    c.item_off = (const uint16_t*)(b + parts[3].off);
-    c.items = (const uint2*)(b + parts[4].off);
-    return CUSAT_OK;
-}
+namespace {
 
 // Decoder engine shared by the plain decoder and the fused chain.
 struct Engine {
@@ -119,7 +52,7 @@ struct Engine {
         memset(&proto, 0, sizeof(proto));
         proto.code = dp.code;
         proto.max_trials = max_trials;
-        cusat::decoder_smem_layout(&proto, p->cmax, n_points);
+        cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, n_points));
         int optin = 0, sms = 0;
         CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
@@ -137,6 +70,7 @@ struct Engine {
         CU(cudaMalloc(&msg, msg_bytes), "cudaMalloc(messages)");
         CU(cudaMalloc(&queue, 256), "cudaMalloc(queue)");
         proto.msg = msg;
+        proto.msg_stride = p->R * p->msg_row / 16;
         proto.queue = queue;
         return CUSAT_OK;
     }
@@ -166,73 +100,7 @@ struct Engine {
     }
 };
 
-struct DevBch {
-    cusat::BchTables t;
-    void* blob = nullptr;
-    cusat::BchDev d{};
-
-    int init(const uint64_t* gen, int p, unsigned n_bytes)
-    {
-        std::string err;
-        if (!cusat::build_bch_tables(gen, p, n_bytes, &t, &err))
-            return fail(CUSAT_ERR_ARG, err);
-        const size_t nl = t.lut.size() * 8, nt = t.tree.size() * 8;
-        CU(cudaMalloc(&blob, nl + nt), "cudaMalloc(bch)");
-        CU(cudaMemcpy(blob, t.lut.data(), nl, cudaMemcpyHostToDevice), "cudaMemcpy(bch)");
-        CU(cudaMemcpy((char*)blob + nl, t.tree.data(), nt, cudaMemcpyHostToDevice), "cudaMemcpy(bch)");
-        d.p = t.p;
-        d.words = t.words;
-        d.n_bytes = t.n_bytes;
-        d.chunk = t.chunk;
-        d.lead = t.lead;
-        d.lut = (const uint64_t*)blob;
-        d.tree = (const uint64_t*)((char*)blob + nl);
-        return CUSAT_OK;
-    }
-    void release()
-    {
-        if (blob)
-            cudaFree(blob);
-        blob = nullptr;
-    }
-};
-
-struct DevDemapObj {
-    cusat::ModcodDemap m;
-    float2* pts = nullptr;
-    cusat::DevDemap d{};
-
-    int init(int mod, int rate, int fs)
-    {
-        std::string err;
-        if (!cusat::build_modcod_demap(mod, rate, fs, &m, &err))
-            return fail(CUSAT_ERR_UNSUPPORTED, err);
-        CU(cudaMalloc(&pts, m.pts.size() * 4), "cudaMalloc(points)");
-        CU(cudaMemcpy(pts, m.pts.data(), m.pts.size() * 4, cudaMemcpyHostToDevice), "cudaMemcpy(points)");
-        d.kind = m.kind;
-        d.n_mod = m.n_mod;
-        d.n_points = m.n_points;
-        d.xfec = m.xfec;
-        d.interleaved_len = m.interleaved_len;
-        d.fec_len = m.fec_len;
-        for (int b = 0; b < 8; b++)
-            d.col[b] = m.col[b];
-        d.points = pts;
-        return CUSAT_OK;
-    }
-    void release()
-    {
-        if (pts)
-            cudaFree(pts);
-        pts = nullptr;
-    }
-};
-
 }  // namespace
-
-namespace cusat {
-void set_last_error(const std::string& msg) { g_last_error = msg; }
-}  // namespace cusat
 
 struct cusat_ldpc_decoder {
     Engine eng;

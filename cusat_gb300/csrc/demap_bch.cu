@@ -118,6 +118,90 @@ __global__ void __launch_bounds__(128) bch_check_kernel(BchDev t, const uint8_t*
     }
 }
 
+// Mixed batches: one warp per frame, each frame with its own code's tables
+// (LUT read through L1 instead of staged in shared memory).
+template <int W>
+__device__ void bch_frame(const BchDev& t, const uint8_t* __restrict__ src, int32_t* valid, int lane)
+{
+    const int p = t.p;
+    const uint64_t top_mask = (p % 64) ? ((1ull << (p % 64)) - 1) : ~0ull;
+    uint64_t r[W];
+#pragma unroll
+    for (int w = 0; w < W; w++)
+        r[w] = 0;
+    const int v0 = lane * t.chunk, v1 = v0 + t.chunk;
+    for (int v = max(v0, (int)t.lead); v < v1; v++) {
+        const unsigned b = src[v - t.lead];
+        const int lo = p - 8;
+        const unsigned idx = b ^ (unsigned)((r[lo >> 6] >> (lo & 63)) & 255);
+#pragma unroll
+        for (int w = W - 1; w >= 0; w--)
+            r[w] = (r[w] << 8) | (w ? r[w - 1] >> 56 : 0);
+        r[W - 1] &= top_mask;
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            r[w] ^= __ldg(t.lut + idx * W + w);
+    }
+    const int nb = p / 8;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        uint64_t o[W], a[W], acc[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            o[w] = __shfl_xor_sync(0xffffffffu, r[w], 1 << k);
+            a[w] = (lane & (1 << k)) ? o[w] : r[w];
+            acc[w] = (lane & (1 << k)) ? r[w] : o[w];
+        }
+        const uint64_t* tk = t.tree + (size_t)k * nb * 256 * W;
+        for (int jb = 0; jb < nb; jb++) {
+            const unsigned byte = (unsigned)((a[jb >> 3] >> ((jb & 7) * 8)) & 255);
+            const uint64_t* e = tk + ((size_t)jb * 256 + byte) * W;
+#pragma unroll
+            for (int w = 0; w < W; w++)
+                acc[w] ^= __ldg(e + w);
+        }
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            r[w] = acc[w];
+    }
+    if (lane == 0) {
+        uint64_t any = 0;
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            any |= r[w];
+        *valid = any == 0;
+    }
+}
+
+__global__ void __launch_bounds__(128) bch_check_mixed_kernel(const BchDev* __restrict__ codes,
+                                                              const BchFrame* __restrict__ frames, int n)
+{
+    const int lane = threadIdx.x & 31;
+    const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (f >= n)
+        return;
+    const BchFrame fr = frames[f];
+    if (!fr.valid)
+        return;
+    const BchDev t = codes[fr.code];
+    if (t.words == 2)
+        bch_frame<2>(t, fr.cw, fr.valid, lane);
+    else if (t.words == 3)
+        bch_frame<3>(t, fr.cw, fr.valid, lane);
+    else if (t.words == 4)
+        bch_frame<4>(t, fr.cw, fr.valid, lane);
+    else
+        bch_frame<1>(t, fr.cw, fr.valid, lane);
+}
+
+int launch_bch_check_mixed(const BchDev* codes, const BchFrame* frames, int n, cudaStream_t stream)
+{
+    if (n <= 0)
+        return 0;
+    bch_check_mixed_kernel<<<(n + 3) / 4, 128, 0, stream>>>(codes, frames, n);
+    return (int)cudaGetLastError();
+}
+
 int launch_bch_check(const BchDev& t, const uint8_t* cw, int32_t* valid, uint8_t* rem, int batch,
                      cudaStream_t stream)
 {

@@ -20,6 +20,13 @@ struct BchDev {
     const uint64_t* tree;  // [5][p/8][256][words]
 };
 
+// One frame of a mixed BCH check.
+struct BchFrame {
+    int code, pad;
+    const uint8_t* cw;
+    int32_t* valid;  // nullptr: frame not checked
+};
+
 // Shared-memory layout and limits of one decoder kernel instantiation.
 struct DecoderKernelInfo {
     const void* fn;
@@ -27,10 +34,16 @@ struct DecoderKernelInfo {
     int blocks_per_sm;
 };
 
-// Fills the shared-memory carve-up of a and returns the kernel to launch
-// (nullptr if the (cmax, lanes) pair has no instantiation).
+// Largest code dimensions a decoder launch must hold in shared memory.
+struct SmemDims {
+    int N, q, n_steps, n_items, cmax, n_points;
+};
+
+// The kernel instantiation for (cmax, lanes, fused), or nullptr.
 const void* select_decoder_kernel(int cmax, int lanes, bool fused);
-void decoder_smem_layout(DecodeArgs* a, int cmax, int n_points);
+// Fills the shared-memory carve-up of a for codes up to d.
+void decoder_smem_layout(DecodeArgs* a, const SmemDims& d);
+SmemDims smem_dims_of(const DevCode& c, int n_points);
 int decoder_threads(int lanes);
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
 
@@ -39,6 +52,7 @@ int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var
 // Sets the message returned by cusat_last_error() on this thread.
 void set_last_error(const std::string& msg);
 
+int launch_bch_check_mixed(const BchDev* codes, const BchFrame* frames, int n, cudaStream_t stream);
 int launch_bch_check(const BchDev& t, const uint8_t* cw, int32_t* valid, uint8_t* rem, int batch,
                      cudaStream_t stream);
 

@@ -35,25 +35,30 @@ const void* select_decoder_kernel(int cmax, int lanes, bool fused)
 
 int decoder_threads(int lanes) { return lanes * kLaneThreads; }
 
-void decoder_smem_layout(DecodeArgs* a, int cmax, int n_points)
+void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
 {
-    const DevCode& c = a->code;
-    int off = align16(c.N * 2 + 2);  // APP + the absent-edge scratch slot
+    int off = align16(d.N * 2 + 2);  // APP + the absent-edge scratch slot
     auto take = [&](int* field, int bytes) {
         *field = off;
         off = align16(off + bytes);
     };
     take(&a->sm_dummy, 2 * kM * 2);  // +32767 region, then the junk region
     take(&a->sm_stage, kStageSets * kMaxStage * kM * 2);
-    take(&a->sm_tab, c.q * cmax * 8);
-    take(&a->sm_cnt, c.q);
-    take(&a->sm_sched, c.n_steps * 4);
-    take(&a->sm_conf, c.n_steps);
-    take(&a->sm_item_off, (c.n_steps + 1) * 2);
-    take(&a->sm_items, c.n_items * 8);
-    take(&a->sm_pts, n_points * 8);
+    take(&a->sm_tab, d.q * d.cmax * 8);
+    take(&a->sm_cnt, d.q);
+    take(&a->sm_sched, d.n_steps * 4);
+    take(&a->sm_conf, d.n_steps);
+    take(&a->sm_item_off, (d.n_steps + 1) * 2);
+    take(&a->sm_items, d.n_items * 8);
+    take(&a->sm_pts, d.n_points * 8);
+    take(&a->sm_code, (int)(sizeof(DevCode) + 8 + sizeof(DevDemap)));
     take(&a->sm_misc, 16);
     a->sm_total = off;
+}
+
+SmemDims smem_dims_of(const DevCode& c, int n_points)
+{
+    return SmemDims{c.N, c.q, c.n_steps, c.n_items, c.cmax, n_points};
 }
 
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream)

@@ -44,20 +44,43 @@
 
 namespace cusat {
 
+// One frame of a mixed batch (device memory).
+struct FrameDesc {
+    int code;                // index into DecodeArgs::codes / demaps
+    float noise_var, llr_gain;
+    int pad;
+    const void* in;          // int16 LLRs [N] or complex symbols [xfec]
+    uint8_t* hard;           // [K/8]
+    int32_t* trials;         // [1]
+};
+
 struct DecodeArgs {
-    DevCode code;
-    DevDemap dm;             // fused demap when sym != nullptr
-    const int16_t* llr;      // [n_frames][N] int16 LLRs (unfused)
-    const float* sym;        // [n_frames][xfec][2] symbols (fused)
+    DevCode code;            // single-code launch (codes == nullptr)
+    DevDemap dm;             // fused demap of the single-code launch
+    const DevCode* codes;    // mixed batch: per-code tables, frames[f].code indexes them
+    const DevDemap* demaps;
+    const FrameDesc* frames;
+    const int16_t* llr;      // single code: [n_frames][N] int16 LLRs (unfused)
+    const float* sym;        // single code: [n_frames][xfec][2] symbols (fused)
     float noise_var, llr_gain;
     int n_frames, max_trials;
-    uint8_t* hard;           // [n_frames][K/8]
-    int32_t* trials;         // [n_frames]
-    uint4* msg;              // [gridDim.x][R * msg_row / 16] scratch
+    uint8_t* hard;           // single code: [n_frames][K/8]
+    int32_t* trials;         // single code: [n_frames]
+    uint4* msg;              // [gridDim.x][msg_stride] scratch
+    int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
     unsigned int* queue;     // frame counter, zero at launch
     const int16_t* weights;  // learned min-sum weights or nullptr (plain)
     // shared-memory carve-up (bytes)
-    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_misc, sm_total;
+    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_code, sm_misc,
+        sm_total;
+};
+
+// Where one frame comes from and goes to.
+struct Job {
+    const void* in;
+    uint8_t* hard;
+    int32_t* trials;
+    float noise_var, llr_gain;
 };
 
 // Shared-memory views of the code tables.
@@ -283,12 +306,11 @@ __device__ __forceinline__ void complete_groups(unsigned char* smem, const int16
 }
 
 template <int CMAX, int LANES, bool SAT>
-__device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, const int16_t* stage, const SmemCode& t,
-                             int f)
+__device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned char* smem, const int16_t* stage,
+                             const SmemCode& t, const Job& job)
 {
     constexpr int NE = CMAX + 2;
     constexpr int RW = (NE + 15) / 16;
-    const DevCode& c = a.code;
     const int tid = threadIdx.x;
     const int lane = (LANES == 2 && tid >= kLaneThreads) ? 1 : 0;
     const int j = tid - lane * kLaneThreads;
@@ -296,7 +318,7 @@ __device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, const int
     const int K = c.K, q = c.q, T = a.max_trials, n_steps = c.n_steps;
     const int pty = 2 * K;         // byte offset of the parity APP
     const int spare = 2 * c.N;     // scratch slot for the absent parity edge
-    uint4* msg_cta = a.msg + (size_t)blockIdx.x * ((size_t)c.R * RW);
+    uint4* msg_cta = a.msg + (size_t)blockIdx.x * (size_t)a.msg_stride;
     int result = -1;
 
     for (int trial = 0;; trial++) {
@@ -342,21 +364,19 @@ __device__ void decode_frame(const DecodeArgs& a, unsigned char* smem, const int
                 cur[w] = nxt[w];
         }
     }
-    pack_hard(reinterpret_cast<const int16_t*>(smem), K, a.hard + (size_t)f * (K / 8));
+    pack_hard(reinterpret_cast<const int16_t*>(smem), K, job.hard);
     if (threadIdx.x == 0)
-        a.trials[f] = result;
+        *job.trials = result;
 }
 
 // Channel LLRs of frame f into shared memory; returns nonzero if one is
 // outside the saturation-free range.  Reference init :655-670 (clamp to
 // +-32767, parity transpose).
-__device__ __forceinline__ int load_llr(const DecodeArgs& a, int16_t* app, int f)
+__device__ __forceinline__ int load_llr(const DevCode& c, int16_t* app, const int16_t* src)
 {
-    const DevCode& c = a.code;
     const int K = c.K, R = c.R, q = c.q, lim = c.fast_lim;
-    const int16_t* src = a.llr + (size_t)f * c.N;
     int over = 0;
-    const bool vec = ((reinterpret_cast<uintptr_t>(a.llr) & 15) == 0);
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
     if (vec) {
         for (int v = threadIdx.x * 8; v < K; v += blockDim.x * 8) {
             const uint4 w = __ldcs(reinterpret_cast<const uint4*>(src + v));
@@ -402,18 +422,16 @@ __device__ __forceinline__ int load_llr(const DecodeArgs& a, int16_t* app, int f
 }
 
 // Fused demap + deinterleave of frame f's symbols straight into the APP.
-__device__ __forceinline__ int demap_into(const DecodeArgs& a, int16_t* app, const float2* pts, int f)
+__device__ __forceinline__ int demap_into(const DevCode& c, const DevDemap& d, int16_t* app, const float2* pts,
+                                          const float2* src, float noise_var, float llr_gain)
 {
-    const DevCode& c = a.code;
-    const DevDemap& d = a.dm;
     const int K = c.K, q = c.q, lim = c.fast_lim, N = c.N;
-    const float2* src = reinterpret_cast<const float2*>(a.sym) + (size_t)f * d.xfec;
     int over = 0;
     for (int jj = threadIdx.x; jj < d.interleaved_len; jj += blockDim.x) {
         const float2 s = __ldcs(src + jj);
         int pos[8];
         int16_t l[8];
-        const int nb = demap_symbol(d, pts, s.x, s.y, jj, a.noise_var, a.llr_gain, pos, l);
+        const int nb = demap_symbol(d, pts, s.x, s.y, jj, noise_var, llr_gain, pos, l);
 #pragma unroll
         for (int b = 0; b < 8; b++) {
             if (b < nb && pos[b] < N) {
@@ -430,13 +448,14 @@ __device__ __forceinline__ int demap_into(const DecodeArgs& a, int16_t* app, con
     return over;
 }
 
-template <int CMAX, int LANES, bool FUSED>
-__global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc_layered_kernel(DecodeArgs a)
+// Copies one code's tables (and demap points) into shared memory; the slot
+// descriptors are rebased onto this kernel's stage and dummy regions and
+// packed to 8 bytes: x = bit base, y = r | store offset << 9.
+template <int CMAX, bool FUSED>
+__device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCode& gc, const DevDemap& gd)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    int16_t* app = reinterpret_cast<int16_t*>(smem);
-    int16_t* dummy = reinterpret_cast<int16_t*>(smem + a.sm_dummy);
-    const int16_t* stage = reinterpret_cast<const int16_t*>(smem + a.sm_stage);
+    DevCode* s_code = reinterpret_cast<DevCode*>(smem + a.sm_code);
+    DevDemap* s_dm = reinterpret_cast<DevDemap*>(smem + a.sm_code + sizeof(DevCode) + 8);
     uint2* s_tab = reinterpret_cast<uint2*>(smem + a.sm_tab);
     uint8_t* s_cnt = smem + a.sm_cnt;
     int16_t* s_sched = reinterpret_cast<int16_t*>(smem + a.sm_sched);
@@ -444,40 +463,56 @@ __global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc
     uint16_t* s_item_off = reinterpret_cast<uint16_t*>(smem + a.sm_item_off);
     uint2* s_items = reinterpret_cast<uint2*>(smem + a.sm_items);
     float2* pts = reinterpret_cast<float2*>(smem + a.sm_pts);
-    int* s_misc = reinterpret_cast<int*>(smem + a.sm_misc);
-    const DevCode& c = a.code;
-
-    // slot descriptors, rebased onto this kernel's stage and dummy regions
-    // and packed to 8 bytes: x = bit base, y = r | store offset << 9
-    for (int k = threadIdx.x; k < c.q * CMAX; k += blockDim.x) {
-        uint4 w = c.tab[k];
+    if (threadIdx.x == 0) {
+        *s_code = gc;
+        *s_dm = gd;
+    }
+    for (int k = threadIdx.x; k < gc.q * CMAX; k += blockDim.x) {
+        uint4 w = gc.tab[k];
         if (w.w == kSlotStaged)
             w.z += (uint32_t)a.sm_stage;
         else if (w.w == kSlotAbsent)
             w.x = (uint32_t)a.sm_dummy;
         s_tab[k] = make_uint2(w.x, w.y | (w.z << 9));
     }
-    for (int k = threadIdx.x; k < c.q; k += blockDim.x) {
+    for (int k = threadIdx.x; k < gc.q; k += blockDim.x) {
         int n = 0;
         for (int e = 0; e < CMAX; e++)
-            n += c.tab[k * CMAX + e].w != kSlotAbsent;
+            n += gc.tab[k * CMAX + e].w != kSlotAbsent;
         s_cnt[k] = (uint8_t)n;
     }
+    for (int k = threadIdx.x; k < 2 * gc.n_steps; k += blockDim.x)
+        s_sched[k] = gc.sched[k];
+    for (int k = threadIdx.x; k < gc.n_steps; k += blockDim.x)
+        s_conf[k] = gc.step_conf[k];
+    for (int k = threadIdx.x; k <= gc.n_steps; k += blockDim.x)
+        s_item_off[k] = gc.item_off[k];
+    for (int k = threadIdx.x; k < gc.n_items; k += blockDim.x)
+        s_items[k] = gc.items[k];
+    if (FUSED && gd.kind == 2)
+        for (int k = threadIdx.x; k < gd.n_points; k += blockDim.x)
+            pts[k] = gd.points[k];
+}
+
+template <int CMAX, int LANES, bool FUSED>
+__global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc_layered_kernel(DecodeArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    int16_t* app = reinterpret_cast<int16_t*>(smem);
+    int16_t* dummy = reinterpret_cast<int16_t*>(smem + a.sm_dummy);
+    const int16_t* stage = reinterpret_cast<const int16_t*>(smem + a.sm_stage);
+    const DevCode& c = *reinterpret_cast<const DevCode*>(smem + a.sm_code);
+    const DevDemap& dm = *reinterpret_cast<const DevDemap*>(smem + a.sm_code + sizeof(DevCode) + 8);
+    const float2* pts = reinterpret_cast<const float2*>(smem + a.sm_pts);
+    int* s_misc = reinterpret_cast<int*>(smem + a.sm_misc);
+    const SmemCode t = {reinterpret_cast<const uint2*>(smem + a.sm_tab), smem + a.sm_cnt,
+                        reinterpret_cast<const int16_t*>(smem + a.sm_sched), smem + a.sm_conf,
+                        reinterpret_cast<const uint16_t*>(smem + a.sm_item_off),
+                        reinterpret_cast<const uint2*>(smem + a.sm_items)};
+
     for (int k = threadIdx.x; k < kM; k += blockDim.x)
         dummy[k] = 32767;  // absent circulants read +32767: never a minimum, no sign
-    for (int k = threadIdx.x; k < 2 * c.n_steps; k += blockDim.x)
-        s_sched[k] = c.sched[k];
-    for (int k = threadIdx.x; k < c.n_steps; k += blockDim.x)
-        s_conf[k] = c.step_conf[k];
-    for (int k = threadIdx.x; k <= c.n_steps; k += blockDim.x)
-        s_item_off[k] = c.item_off[k];
-    for (int k = threadIdx.x; k < c.n_items; k += blockDim.x)
-        s_items[k] = c.items[k];
-    if (FUSED && a.dm.kind == 2)
-        for (int k = threadIdx.x; k < a.dm.n_points; k += blockDim.x)
-            pts[k] = a.dm.points[k];
-    const SmemCode t = {s_tab, s_cnt, s_sched, s_conf, s_item_off, s_items};
-
+    int loaded = -1;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0)
@@ -486,11 +521,35 @@ __global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc
         const int f = s_misc[0];
         if (f >= a.n_frames)
             break;
-        const int over = FUSED ? demap_into(a, app, pts, f) : load_llr(a, app, f);
+        Job job;
+        int code_id = 0;
+        if (a.frames) {
+            const FrameDesc fd = a.frames[f];
+            code_id = fd.code;
+            job = {fd.in, fd.hard, fd.trials, fd.noise_var, fd.llr_gain};
+        }
+        if (code_id != loaded) {
+            if (a.codes)
+                load_code<CMAX, FUSED>(a, smem, a.codes[code_id], FUSED ? a.demaps[code_id] : a.dm);
+            else
+                load_code<CMAX, FUSED>(a, smem, a.code, a.dm);
+            loaded = code_id;
+            __syncthreads();
+        }
+        if (!a.frames) {
+            job.in = FUSED ? (const void*)(a.sym + (size_t)f * 2 * dm.xfec) : (const void*)(a.llr + (size_t)f * c.N);
+            job.hard = a.hard + (size_t)f * (c.K / 8);
+            job.trials = a.trials + f;
+            job.noise_var = a.noise_var;
+            job.llr_gain = a.llr_gain;
+        }
+        const int over = FUSED ? demap_into(c, dm, app, pts, reinterpret_cast<const float2*>(job.in), job.noise_var,
+                                            job.llr_gain)
+                               : load_llr(c, app, reinterpret_cast<const int16_t*>(job.in));
         if (__syncthreads_or(over))
-            decode_frame<CMAX, LANES, true>(a, smem, stage, t, f);
+            decode_frame<CMAX, LANES, true>(a, c, smem, stage, t, job);
         else
-            decode_frame<CMAX, LANES, false>(a, smem, stage, t, f);
+            decode_frame<CMAX, LANES, false>(a, c, smem, stage, t, job);
     }
 }
 

@@ -174,8 +174,9 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     a.hard = hard_out;
     a.trials = trials_out;
     a.msg = (uint4*)st.msg;
+    a.msg_stride = p->R * p->msg_row / 16;
     a.queue = st.queue;
-    cusat::decoder_smem_layout(&a, p->cmax, 0);
+    cusat::decoder_smem_layout(&a, cusat::smem_dims_of(a.code, 0));
     if (a.sm_total > st.optin)
         return fail(CUSAT_ERR_UNSUPPORTED, "frame state does not fit in shared memory");
     const void* fn = cusat::select_decoder_kernel(p->cmax, p->lanes, false);

@@ -171,6 +171,48 @@ int cusat_rx_fec_launch(cusat_rx_fec* rx, const float* sym_dev, int batch, float
                         int32_t* bch_valid_out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Mixed-MODCOD batches                                                    */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_batch cusat_batch;
+
+/* One frame of a mixed batch. */
+typedef struct {
+    int32_t modcod;       /* index into the MODCOD list given at creation */
+    float noise_var;      /* N0 of this frame (QPSK LLR scale) */
+    float llr_gain;       /* gain for 8PSK/APSK, capped like demap_batch */
+    int32_t reserved;
+    const float* sym;     /* device: xfecframe_len complex symbols (re, im) */
+    uint8_t* hard;        /* device or mapped pinned: k_ldpc/8 bytes */
+    int32_t* trials;      /* device or mapped pinned: one int */
+    int32_t* bch_valid;   /* device or mapped pinned: one int, or NULL */
+} cusat_frame;
+
+/* No counterpart in the reference, which builds one chain per MODCOD and
+ * flushes on every MODCOD change (lib/cusat_dsp/rx_fec_pool.cc:48-87).  A
+ * batch decodes frames of any of the given MODCODs (modcods: n triples
+ * modulation, rate, frame size) in one launch sequence: fused demap ->
+ * decode -> BCH; each frame's results equal those of a single-MODCOD
+ * cusat_rx_fec launch on the same symbols. */
+int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, int max_frames,
+                       cusat_batch** out);
+void cusat_batch_destroy(cusat_batch* b);
+/* out[0..3] = MODCODs, kernel classes, max_frames, max_trials */
+int cusat_batch_info(const cusat_batch* b, int32_t* out);
+/* Decodes n frames on `stream` (waits for the previous launch's descriptor
+ * copies first; the frames' buffers must stay valid until completion). */
+int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* stream);
+/* Times reps launches of each candidate (class order x grid split) on this
+ * frame list and keeps the fastest for later launches and captures. */
+int cusat_batch_tune(cusat_batch* b, const cusat_frame* frames, int n, int reps, void* stream,
+                     float* best_ms);
+/* Captures the launch sequence for this frame list into a CUDA graph
+ * (stream must not be the legacy default stream); cusat_batch_replay
+ * relaunches it: same frames, same buffers, whatever they hold now. */
+int cusat_batch_capture(cusat_batch* b, const cusat_frame* frames, int n, void* stream);
+int cusat_batch_replay(cusat_batch* b, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Decoding without device allocation                                      */
 /* ---------------------------------------------------------------------- */
 
