@@ -122,6 +122,15 @@ def map_frames(modulation, rate, framesize, cw):
     return sym
 
 
+
+def _weights_arg(weights):
+    """(pointer, n_iter, keep-alive array) for a learned weight table
+    ([n_iter, 32, 2] int16 {beta, alpha/64}) or None (plain decoder)."""
+    if weights is None:
+        return None, 0, None
+    w = np.ascontiguousarray(np.asarray(weights, np.int16).reshape(-1, 32, 2))
+    return w.ctypes.data, w.shape[0], w
+
 class ldpc_decode_cuda:
     """Layered min-sum LDPC decoder (reference cuda::ldpc_decode_cuda).
 
@@ -157,6 +166,11 @@ class ldpc_decode_cuda:
     def decode_launch_async(self, soft_in, batch_size, stream=None, hard_out=None, result_out=None):
         _capi.check(_capi.lib().cusat_ldpc_decode_launch(self._h, _addr(soft_in), batch_size, _stream(stream),
                                                           _addr(hard_out), _addr(result_out)))
+
+    def set_weights(self, weights):
+        """Learned min-sum weights ([n_iter, 32, 2] int16 {beta, alpha/64}) or None."""
+        p, n, _keep = _weights_arg(weights)
+        _capi.check(_capi.lib().cusat_ldpc_decoder_set_weights(self._h, p, n))
 
     def results(self, batch_size):
         hard = np.zeros((batch_size, self._kb), np.uint8)
@@ -313,6 +327,11 @@ class rx_fec:
     def capped_llr_gain(self, llr_gain):
         return float(_capi.lib().cusat_rx_fec_capped_llr_gain(self._h, llr_gain))
 
+    def set_weights(self, weights):
+        """Learned min-sum weights ([n_iter, 32, 2] int16 {beta, alpha/64}) or None."""
+        p, n, _keep = _weights_arg(weights)
+        _capi.check(_capi.lib().cusat_rx_fec_set_weights(self._h, p, n))
+
     def launch(self, sym_dev, batch_size, noise_var, llr_gain, hard_out, trials_out, bch_valid_out=None,
                stream=None):
         _capi.check(_capi.lib().cusat_rx_fec_launch(self._h, _addr(sym_dev), batch_size, noise_var, llr_gain,
@@ -345,6 +364,11 @@ class batch:
 
     def info(self):
         return _info(_capi.lib().cusat_batch_info, self._h, 4)
+
+    def set_weights(self, modcod, weights):
+        """Learned weights for MODCOD index `modcod` of this batch, or None."""
+        p, n, _keep = _weights_arg(weights)
+        _capi.check(_capi.lib().cusat_batch_set_weights(self._h, modcod, p, n))
 
     @staticmethod
     def frames(modcod, noise_var, llr_gain, sym, hard, trials, bch_valid=None):

@@ -20,6 +20,7 @@ _SIGS = {
                                                   ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_ldpc_decoder_destroy": (None, [ctypes.c_void_p]),
     "cusat_ldpc_decoder_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_ldpc_decoder_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_ldpc_decode_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "cusat_ldpc_decode_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -52,16 +53,24 @@ _SIGS = {
                                            ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_rx_fec_destroy": (None, [ctypes.c_void_p]),
     "cusat_rx_fec_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_rx_fec_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_rx_fec_capped_llr_gain": (ctypes.c_float, [ctypes.c_void_p, ctypes.c_float]),
     "cusat_rx_fec_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),
+    "cusat_nms_trainer_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_nms_trainer_destroy": (None, [ctypes.c_void_p]),
+    "cusat_nms_trainer_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_nms_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "cusat_ldpc_decode_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "cusat_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_batch_destroy": (None, [ctypes.c_void_p]),
     "cusat_batch_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_batch_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "cusat_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "cusat_batch_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),

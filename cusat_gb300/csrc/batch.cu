@@ -27,6 +27,7 @@ struct ModcodObj {
     DevPlan dp;
     DevDemapObj dm;
     DevBch bch;
+    DevWeights weights;
     int cls = -1;       // kernel class
     int code_in_class = 0;
 };
@@ -91,6 +92,7 @@ void release(cusat_batch* b)
         m->dp.blob ? (void)cudaFree(m->dp.blob) : (void)0;
         m->dm.release();
         m->bch.release();
+        m->weights.release();
     }
     if (b->h_frames) cudaFreeHost(b->h_frames);
     if (b->h_bch) cudaFreeHost(b->h_bch);
@@ -338,6 +340,44 @@ int cusat_batch_info(const cusat_batch* b, int32_t* out)
     out[3] = b->max_trials;
     return CUSAT_OK;
 }
+
+int cusat_batch_set_weights(cusat_batch* b, int modcod, const int16_t* weights, int n_iter)
+{
+    if (!b || modcod < 0 || modcod >= (int)b->modcods.size())
+        return fail(CUSAT_ERR_ARG, "unknown MODCOD index");
+    ModcodObj& m = *b->modcods[modcod];
+    cusat::DevCode dc = m.dp.code;
+    CU(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    if (weights) {
+        const int rc = m.weights.set(weights, n_iter, b->max_trials);
+        if (rc)
+            return rc;
+        dc.weights = m.weights.d;
+    }
+    KernelClass& c = b->classes[m.cls];
+    CU(cudaMemcpy(c.d_codes + m.code_in_class, &dc, sizeof(dc), cudaMemcpyHostToDevice), "cudaMemcpy(code)");
+    return CUSAT_OK;
+}
+
+}  // extern "C"
+
+namespace cusat_internal {
+
+// Launch for callers that know the object's previous launch has completed
+// (its staging buffers are free): no stream synchronisation.
+int batch_launch_ready(cusat_batch* b, const cusat_frame* frames, int n, cudaStream_t stream)
+{
+    if (!b || !frames || n <= 0 || n > b->max_frames)
+        return fail(CUSAT_ERR_ARG, "frames outside 1..max_frames");
+    const int rc = stage(b, frames, n);
+    if (rc)
+        return rc;
+    return enqueue(b, n, stream, b->d_frames, b->d_bch, true);
+}
+
+}  // namespace cusat_internal
+
+extern "C" {
 
 int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* stream)
 {

@@ -33,6 +33,21 @@ struct Engine {
     cusat::DecodeArgs proto{};
     uint4* msg = nullptr;
     unsigned int* queue = nullptr;
+    DevWeights weights;
+
+    int set_weights(const int16_t* w, int n_iter)
+    {
+        if (!w) {
+            proto.code.weights = nullptr;
+            return CUSAT_OK;
+        }
+        CU(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        const int rc = weights.set(w, n_iter, max_trials);
+        if (rc)
+            return rc;
+        proto.code.weights = weights.d;
+        return CUSAT_OK;
+    }
 
     int init(const cusat::CodePlan* p, int trials, int batch, bool fused, int n_points)
     {
@@ -94,6 +109,7 @@ struct Engine {
             cudaFree(msg);
         if (queue)
             cudaFree(queue);
+        weights.release();
         dp.blob = nullptr;
         msg = nullptr;
         queue = nullptr;
@@ -176,6 +192,13 @@ void cusat_ldpc_decoder_destroy(cusat_ldpc_decoder* d)
     if (d->trials_pinned)
         cudaFreeHost(d->trials_pinned);
     delete d;
+}
+
+int cusat_ldpc_decoder_set_weights(cusat_ldpc_decoder* d, const int16_t* weights, int n_iter)
+{
+    if (!d)
+        return fail(CUSAT_ERR_ARG, "null decoder");
+    return d->eng.set_weights(weights, n_iter);
 }
 
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* d, int32_t* out)
@@ -473,6 +496,13 @@ void cusat_rx_fec_destroy(cusat_rx_fec* r)
     r->dm.release();
     r->bch.release();
     delete r;
+}
+
+int cusat_rx_fec_set_weights(cusat_rx_fec* r, const int16_t* weights, int n_iter)
+{
+    if (!r)
+        return fail(CUSAT_ERR_ARG, "null chain");
+    return r->eng.set_weights(weights, n_iter);
 }
 
 int cusat_rx_fec_info(const cusat_rx_fec* r, int32_t* out)

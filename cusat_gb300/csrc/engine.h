@@ -45,6 +45,53 @@ inline int require_device(int* dev)
     return CUSAT_OK;
 }
 
+// Learned min-sum weights: validates n_iter rows of [32][2] {beta, alpha in
+// 64ths} and expands them to `rows` rows (later rows repeat the last one).
+inline int weight_table(const int16_t* w, int n_iter, int rows, std::vector<int16_t>* out)
+{
+    if (!w || n_iter <= 0)
+        return fail(CUSAT_ERR_ARG, "weights need at least one iteration row");
+    for (int i = 0; i < n_iter * 32; i++)
+        if (w[2 * i] < 0 || w[2 * i] > 127 || w[2 * i + 1] < 0 || w[2 * i + 1] > 255)
+            return fail(CUSAT_ERR_ARG, "weight outside beta 0..127, alpha 0..255");
+    rows = rows < 1 ? 1 : rows;
+    out->resize((size_t)rows * 64);
+    for (int t = 0; t < rows; t++)
+        memcpy(out->data() + (size_t)t * 64, w + (size_t)(t < n_iter ? t : n_iter - 1) * 64, 64 * sizeof(int16_t));
+    return CUSAT_OK;
+}
+
+// Device weight table of one code; set() replaces it, clear() returns to the
+// plain decoder.  Callers make sure no launch that reads it is in flight.
+struct DevWeights {
+    int16_t* d = nullptr;
+    int rows = 0;
+
+    int set(const int16_t* w, int n_iter, int max_trials)
+    {
+        std::vector<int16_t> tab;
+        int rc = weight_table(w, n_iter, max_trials, &tab);
+        if (rc)
+            return rc;
+        if (!d || rows * 64 < (int)tab.size()) {
+            if (d)
+                cudaFree(d);
+            d = nullptr;
+            CU(cudaMalloc(&d, tab.size() * sizeof(int16_t)), "cudaMalloc(weights)");
+            rows = (int)tab.size() / 64;
+        }
+        CU(cudaMemcpy(d, tab.data(), tab.size() * sizeof(int16_t), cudaMemcpyHostToDevice), "cudaMemcpy(weights)");
+        return CUSAT_OK;
+    }
+    void release()
+    {
+        if (d)
+            cudaFree(d);
+        d = nullptr;
+        rows = 0;
+    }
+};
+
 // Device copy of a code plan (one allocation).
 struct DevPlan {
     void* blob = nullptr;
@@ -150,5 +197,10 @@ struct DevDemapObj {
         pts = nullptr;
     }
 };
+
+// Mixed-MODCOD batch launch without the stream synchronisation of
+// cusat_batch_launch (batch.cu); the caller guarantees that the object's
+// previous launch has completed.
+int batch_launch_ready(cusat_batch* b, const cusat_frame* frames, int n, cudaStream_t stream);
 
 }  // namespace cusat_internal

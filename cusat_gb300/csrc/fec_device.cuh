@@ -21,6 +21,9 @@ struct DevCode {
     const uint8_t* step_conf;  // [n_steps] 0, kConfDefer or kConfMid
     const uint16_t* item_off;  // [n_steps + 1] group items of step s
     const uint2* items;        // [n_items]
+    // learned min-sum weights [max_trials][32][2] = {beta, alpha in 64ths}
+    // per (iteration, check degree); nullptr = plain offset min-sum
+    const int16_t* weights;
 };
 
 // Demapper parameters of one MODCOD (points live in device memory).

@@ -69,7 +69,6 @@ struct DecodeArgs {
     uint4* msg;              // [gridDim.x][msg_stride] scratch
     int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
     unsigned int* queue;     // frame counter, zero at launch
-    const int16_t* weights;  // learned min-sum weights or nullptr (plain)
     // shared-memory carve-up (bytes)
     int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_code, sm_misc,
         sm_total;
@@ -206,7 +205,7 @@ __device__ __forceinline__ int scaled_mag(int r, int beta, int alpha)
 // row; straight-line code for every layer (plain, staged and absent slots
 // differ only in their descriptors).
 template <int CMAX, int RW, bool SAT>
-__device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char* smem, const uint2* tb, int cnt,
+__device__ __forceinline__ void process_check(const int16_t* wts, unsigned char* smem, const uint2* tb, int cnt,
                                               int j, int ps0, int ps1, bool absent, const uint4 (&cur)[RW],
                                               uint4* dst, int trial)
 {
@@ -241,9 +240,9 @@ __device__ __forceinline__ void process_check(const DecodeArgs& a, unsigned char
         sx ^= d[e];
     }
     int m1, m2;
-    if (a.weights) {
+    if (wts) {
         const int deg = cnt + (absent ? 1 : 2);
-        const int16_t* w = a.weights + ((size_t)trial * 32 + deg) * 2;
+        const int16_t* w = wts + ((size_t)trial * 32 + deg) * 2;
         m1 = scaled_mag(r1, w[0], w[1]);
         m2 = scaled_mag(r2, w[0], w[1]);
     } else {
@@ -349,7 +348,7 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
                     const int ps0 = pty + 2 * (i * kM + j);
                     const bool absent = (i == 0 && j == 0);
                     const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? spare : pty + 2 * ((q - 1) * kM + j - 1));
-                    process_check<CMAX, RW, SAT>(a, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent, cur,
+                    process_check<CMAX, RW, SAT>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent, cur,
                                                  msg_cta + ((size_t)i * kM + j) * RW, trial);
                 }
             }

@@ -1,0 +1,221 @@
+"""Learned min-sum weights: training, quantisation, persistence, FER.
+
+The weights are one {beta, alpha} pair per decoding iteration and check
+degree.  They are trained in FP32 on the GPU by this library's unrolled
+forward/backward kernels (cusat_nms_train_step) on frames generated by this
+package's BCH/LDPC encoder, mapper, an AWGN channel and the library's soft
+demapper; then quantised into the integer decoder's table (beta in LLR
+units, alpha in 64ths; cusat_*_set_weights).  The plain offset min-sum
+decoder (beta 1, no scaling) stays the fallback: a MODCOD without a weight
+file decodes plain.
+
+The reference has no learned decoder; its normalised-min-sum hook
+(ldpc_decode_kernel.cu:75-90, alpha in 64ths, odd-symmetric rounding) is the
+integer form used here.
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+
+from . import _capi, code_info, encode_frames, map_frames, modcod_info
+from .enums import find_modcod
+
+WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
+
+
+class nms_trainer:
+    """The FP32 unrolled model of one code on the GPU (forward + backward)."""
+
+    def __init__(self, framesize, rate, n_iter, max_batch):
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_nms_trainer_create(framesize, rate, n_iter, max_batch, ctypes.byref(h)))
+        self._h = h
+        out = (ctypes.c_int32 * 6)()
+        _capi.check(_capi.lib().cusat_nms_trainer_info(h, out))
+        self.n_ldpc, self.k_ldpc, self.n_iter, self.max_batch, self.deg_lo, self.deg_hi = list(out)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_nms_trainer_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def step(self, llr, cw, batch, theta, grad, loss, stream=None):
+        """Adds the summed loss (and gradient, unless grad is None) of `batch`
+        frames; all arguments are device tensors or addresses."""
+        from . import _addr, _stream
+        _capi.check(_capi.lib().cusat_nms_train_step(self._h, _addr(llr), _addr(cw), batch, _addr(theta),
+                                                     _addr(grad), _addr(loss), _stream(stream)))
+
+
+def plain_theta(n_iter):
+    """{beta, alpha} of the plain offset min-sum decoder for every entry."""
+    th = np.zeros((n_iter, 32, 2), np.float32)
+    th[:, :, 0] = 1.0
+    th[:, :, 1] = 1.0
+    return th
+
+
+def quantize(theta):
+    """FP32 {beta, alpha} -> the integer decoder's {beta, alpha in 64ths}."""
+    th = np.asarray(theta, np.float32)
+    w = np.zeros(th.shape, np.int16)
+    w[..., 0] = np.clip(np.rint(th[..., 0]), 0, 127)
+    w[..., 1] = np.clip(np.rint(th[..., 1] * 64.0), 1, 255)
+    return w
+
+
+def dequantize(w):
+    w = np.asarray(w)
+    th = np.zeros(w.shape, np.float32)
+    th[..., 0] = w[..., 0]
+    th[..., 1] = np.where(w[..., 1] > 0, w[..., 1] / 64.0, 1.0)
+    return th
+
+
+def weights_path(name, framesize):
+    return os.path.join(WEIGHTS_DIR, f"{name.replace('/', '_')}_{'short' if framesize == 1 else 'normal'}.json")
+
+
+def save_weights(path, name, framesize, w, meta):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    w = np.asarray(w, np.int16)
+    doc = {"modcod": name, "framesize": int(framesize), "n_iter": int(w.shape[0]),
+           "layout": "[n_iter][32 check degrees][beta, alpha/64]", "weights": w.tolist(), "meta": meta}
+    with open(path, "w") as f:
+        json.dump(doc, f, indent=1)
+
+
+def load_weights(name, framesize, path=None):
+    """The stored int16 table [n_iter, 32, 2], or None (decode plain)."""
+    path = path or weights_path(name, framesize)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        doc = json.load(f)
+    return np.asarray(doc["weights"], np.int16)
+
+
+class ChannelPool:
+    """Noisy frames of one MODCOD made on the GPU: a pool of encoded and
+    mapped codewords (unit average symbol energy), fresh AWGN per frame
+    (N0 = 1/SNR, sigma = sqrt(N0/2) per component), demapped by the
+    library's demapper with llr_gain = min(4/N0, 1000) (the conventions of
+    the reference's apps/bench_coded_modulation.cc:287-308,373-391)."""
+
+    def __init__(self, name, framesize, n_codewords, seed, max_batch, torch):
+        from . import demapper_cuda
+        self.torch = torch
+        _, self.mod, self.rate, _, _, self.threshold = find_modcod(name)
+        self.fs = framesize
+        ci = code_info(framesize, self.rate)
+        self.n, self.k_bch = ci["n_ldpc"], ci["k_bch"]
+        rng = np.random.default_rng(seed)
+        msg = rng.integers(0, 256, (n_codewords, self.k_bch // 8), dtype=np.uint8)
+        cw = encode_frames(framesize, self.rate, msg)
+        sym = map_frames(self.mod, self.rate, framesize, cw)
+        es = np.mean(sym.astype(np.float64)[:, 0::2] ** 2 + sym.astype(np.float64)[:, 1::2] ** 2)
+        sym = (sym * np.float32(1.0 / np.sqrt(es))).astype(np.float32)
+        self.cw = torch.from_numpy(cw).cuda()
+        self.sym = torch.from_numpy(sym).cuda()
+        self.dm = demapper_cuda(self.mod, self.rate, framesize, max_batch)
+        self.max_batch = max_batch
+        self.gen = torch.Generator(device="cuda")
+        self.gen.manual_seed(seed)
+
+    def draw(self, batch, esn0_db, stream=None):
+        """(noisy symbols, int16 LLRs, codewords) of `batch` frames, device."""
+        torch = self.torch
+        n0 = float(np.float32(1.0 / 10 ** (esn0_db / 10.0)))
+        sigma = float(np.sqrt(n0 / 2.0))
+        idx = torch.randint(0, self.cw.shape[0], (batch,), device="cuda", generator=self.gen)
+        sym = self.sym[idx] + sigma * torch.randn(batch, self.sym.shape[1], device="cuda", generator=self.gen)
+        llr = torch.empty((batch, self.n), dtype=torch.int16, device="cuda")
+        gain = min(4.0 / n0, 1000.0)
+        # the fused chain caps the gain the same way (demapper_kernel.cu:283-291)
+        self.dm.demap_launch(sym, batch, n0, self.dm.capped_llr_gain(gain), llr,
+                             stream or torch.cuda.current_stream())
+        return sym, llr, self.cw[idx], n0, gain
+
+
+def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128, lr=0.02, seed=1,
+          n_codewords=256, log_every=0, log=print):
+    """Trains {beta, alpha}[n_iter][degree] for one MODCOD; returns
+    (theta float32 [n_iter, 32, 2], history of (frames, mean loss))."""
+    import torch
+    thr = find_modcod(name)[5]
+    if esn0_grid is None:
+        esn0_grid = [thr - 0.5 + 0.25 * k for k in range(7)]
+    pool = ChannelPool(name, framesize, n_codewords, seed, batch, torch)
+    tr = nms_trainer(framesize, pool.rate, n_iter, batch)
+    theta = torch.from_numpy(plain_theta(n_iter)).cuda().requires_grad_(False)
+    grad = torch.zeros_like(theta)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    m = torch.zeros_like(theta)
+    v = torch.zeros_like(theta)
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    used = torch.zeros((32,), dtype=torch.bool)
+    used[tr.deg_lo:tr.deg_hi + 1] = True
+    mask = used.cuda().view(1, 32, 1).expand_as(theta).float()
+    history, acc, acc_n = [], 0.0, 0
+    steps = max(1, n_frames // batch)
+    for k in range(steps):
+        esn0 = esn0_grid[k % len(esn0_grid)]
+        _, llr, cw, _, _ = pool.draw(batch, esn0)
+        grad.zero_()
+        loss.zero_()
+        tr.step(llr, cw, batch, theta, grad, loss)
+        g = grad * mask / batch
+        m.mul_(b1).add_(g, alpha=1 - b1)
+        v.mul_(b2).addcmul_(g, g, value=1 - b2)
+        mh = m / (1 - b1 ** (k + 1))
+        vh = v / (1 - b2 ** (k + 1))
+        theta.sub_(lr * mh / (vh.sqrt() + eps))
+        theta[:, :, 0].clamp_(0.0, 16.0)
+        theta[:, :, 1].clamp_(1.0 / 64.0, 2.0)
+        acc += float(loss.item()) / batch
+        acc_n += 1
+        if log_every and (k + 1) % log_every == 0:
+            history.append(((k + 1) * batch, acc / acc_n))
+            if log:
+                log(f"{name} frames {(k + 1) * batch} loss {acc / acc_n:.5f}")
+            acc, acc_n = 0.0, 0
+    if acc_n:
+        history.append((steps * batch, acc / acc_n))
+    return theta.cpu().numpy(), history
+
+
+def frame_errors(name, framesize, esn0_db, n_iter, weights, n_frames, batch=256, seed=7, min_errors=None,
+                 stream=None):
+    """Frame error rate of the integer decoder (fused chain) with `weights`
+    (None = plain) at `n_iter` maximum iterations on fresh noisy frames.
+    A frame is in error when its decoded k_ldpc bits differ from the sent
+    ones.  Stops early after `min_errors` frame errors.  Returns a dict."""
+    import torch
+    from . import rx_fec
+    pool = ChannelPool(name, framesize, 256, seed, batch, torch)
+    rx = rx_fec(pool.mod, pool.rate, framesize, n_iter, batch)
+    rx.set_weights(weights)
+    kb = rx.k_bytes
+    hard = torch.zeros((batch, kb), dtype=torch.uint8, device="cuda")
+    trials = torch.zeros(batch, dtype=torch.int32, device="cuda")
+    frames = errors = fails = 0
+    iters = 0
+    st = stream or torch.cuda.current_stream()
+    while frames < n_frames:
+        b = min(batch, n_frames - frames)
+        sym, _, cw, n0, gain = pool.draw(b, esn0_db, st)
+        rx.launch(sym, b, n0, gain, hard, trials, None, st)
+        bad = (hard[:b] != cw[:, :kb]).any(dim=1)
+        t = trials[:b]
+        errors += int(bad.sum().item())
+        fails += int((t < 0).sum().item())
+        iters += int(torch.where(t >= 0, n_iter - t, torch.full_like(t, n_iter)).sum().item())
+        frames += b
+        if min_errors and errors >= min_errors:
+            break
+    return {"esn0_db": esn0_db, "frames": frames, "frame_errors": errors, "fer": errors / frames,
+            "decoder_failures": fails, "mean_iterations": iters / frames}

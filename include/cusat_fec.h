@@ -60,6 +60,18 @@ void cusat_ldpc_decoder_destroy(cusat_ldpc_decoder* dec);
  * lanes (2 = paired-layer schedule) */
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* dec, int32_t* out);
 
+/* Learned min-sum weights (no counterpart in the reference, whose
+ * normalised-min-sum hook nms_scale, ldpc_decode_kernel.cu:75-90, is never
+ * enabled).  weights[(t * 32 + d) * 2 + {0, 1}] = {beta, alpha} for
+ * iteration t < n_iter and check degree d: the check-to-bit magnitude
+ * becomes min(((max(m - beta, 0) * alpha + 32) >> 6), 127) instead of
+ * min(max(m - 1, 0), 127), with m the smallest |extrinsic| of the other edges
+ * and alpha in 64ths (0 = no scaling); iterations past n_iter reuse the last
+ * row.  beta in 0..127, alpha in 0..255.  weights == NULL returns to the
+ * plain decoder.  Waits for the device to go idle before replacing the
+ * table. */
+int cusat_ldpc_decoder_set_weights(cusat_ldpc_decoder* dec, const int16_t* weights, int n_iter);
+
 /* Replaces ldpc_decode_cuda::decode_launch_async (ldpc_decode_kernel.cuh:51-64,
  * .cu:1324-1336): decodes `batch` frames of n_bits int16 LLRs read from
  * device memory, asynchronously on `stream`.  hard_out (batch*k_bytes) and
@@ -163,6 +175,8 @@ int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials,
 void cusat_rx_fec_destroy(cusat_rx_fec* rx);
 /* out[0..5] = xfecframe_len, n_bits, k_bits, k_bytes, k_bch, n_mod */
 int cusat_rx_fec_info(const cusat_rx_fec* rx, int32_t* out);
+/* Learned weights for the chain's decoder (see cusat_ldpc_decoder_set_weights). */
+int cusat_rx_fec_set_weights(cusat_rx_fec* rx, const int16_t* weights, int n_iter);
 float cusat_rx_fec_capped_llr_gain(const cusat_rx_fec* rx, float llr_gain);
 /* Symbols on the device in, results to device or mapped pinned memory;
  * llr_gain is capped like demap_batch does (demapper_kernel.cu:283-291). */
@@ -199,6 +213,9 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
 void cusat_batch_destroy(cusat_batch* b);
 /* out[0..3] = MODCODs, kernel classes, max_frames, max_trials */
 int cusat_batch_info(const cusat_batch* b, int32_t* out);
+/* Learned weights for one MODCOD of the batch (NULL: plain); takes effect
+ * for later launches and for replays of an existing capture. */
+int cusat_batch_set_weights(cusat_batch* b, int modcod, const int16_t* weights, int n_iter);
 /* Decodes n frames on `stream` (waits for the previous launch's descriptor
  * copies first; the frames' buffers must stay valid until completion). */
 int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* stream);
@@ -211,6 +228,88 @@ int cusat_batch_tune(cusat_batch* b, const cusat_frame* frames, int n, int reps,
  * relaunches it: same frames, same buffers, whatever they hold now. */
 int cusat_batch_capture(cusat_batch* b, const cusat_frame* frames, int n, void* stream);
 int cusat_batch_replay(cusat_batch* b, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Serving loop                                                            */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_server cusat_server;
+
+#define CUSAT_REQ_HOST_SYMBOLS 1  /* request flag: sym is host memory */
+
+/* One frame request. */
+typedef struct {
+    int32_t modcod;       /* index into the server's MODCOD list */
+    float noise_var;
+    float llr_gain;       /* capped like demap_batch */
+    int32_t flags;        /* CUSAT_REQ_* */
+    const float* sym;     /* xfecframe_len complex symbols, device (default) or
+                             host; read when the frame is admitted, must stay
+                             valid until its result is returned */
+    uint8_t* hard_host;   /* k_ldpc/8 bytes of host memory for the hard
+                             decisions, or NULL */
+    uint64_t tag;         /* returned with the result */
+    double arrival_s;     /* server clock (cusat_server_now); the frame is
+                             not admitted before; < 0: now */
+} cusat_request;
+
+typedef struct {
+    uint64_t tag;
+    int32_t modcod, trials, bch_valid, reserved;
+    double arrival_s, admit_s, done_s;  /* server clock, seconds */
+} cusat_result;
+
+/* No counterpart in the reference (its RX chain pool runs a fixed flight
+ * ring per MODCOD chain, lib/cusat_dsp/rx_fec_chain.cc:281-627).  A
+ * scheduler thread admits arrived requests, in order, into an arena of
+ * hbm_budget device bytes (per frame: its symbols, hard decisions, two
+ * counters) and launches them as mixed-MODCOD batches of at most max_batch
+ * frames on `slots` streams; batches overlap on the device and requests
+ * that arrive meanwhile join the next batch when a slot and memory free up.
+ * Each frame's results equal those of a single-MODCOD cusat_rx_fec launch on
+ * its symbols, whatever it was batched with. */
+int cusat_server_create(const int32_t* modcods, int n_modcods, int max_trials, size_t hbm_budget, int slots,
+                        int max_batch, cusat_server** out);
+/* Stops the scheduler (requests not yet completed are dropped). */
+void cusat_server_destroy(cusat_server* srv);
+double cusat_server_now(const cusat_server* srv);
+/* Learned weights (NULL: plain) for one MODCOD; only while nothing is
+ * pending or in flight. */
+int cusat_server_set_weights(cusat_server* srv, int modcod, const int16_t* weights, int n_iter);
+/* Queues n requests (thread-safe); admitted in submission order once their
+ * arrival time has passed. */
+int cusat_server_submit(cusat_server* srv, const cusat_request* reqs, int n);
+/* Up to max completed results, waiting up to wait_ms for the first; returns
+ * the count or a negative error (a failed launch stops the server). */
+int cusat_server_poll(cusat_server* srv, cusat_result* out, int max, int wait_ms);
+/* out[0..7] = pending, batches launched, frames launched, largest batch,
+ * most batches in flight, peak arena bytes, arena bytes, batches in flight */
+int cusat_server_stats(cusat_server* srv, double* out);
+
+/* ---------------------------------------------------------------------- */
+/* Training the learned min-sum weights                                    */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_nms_trainer cusat_nms_trainer;
+
+/* No counterpart in the reference.  The unrolled FP32 model of the layered
+ * decoder with learnable {beta, alpha} per iteration (n_iter <= 64) and
+ * check degree: per check, m_e = sign product of the other edges *
+ * min(alpha * max(r_e - beta, 0), 127), r_e the smallest |extrinsic| of the
+ * other edges; the reference's paired-layer schedule; loss = mean over
+ * iterations and bits of softplus(-y L) (y = +1 for a 0 bit, L the APP after
+ * the iteration).  Forward and backward run on the GPU, one CTA per frame. */
+int cusat_nms_trainer_create(int framesize, int rate, int n_iter, int max_batch, cusat_nms_trainer** out);
+void cusat_nms_trainer_destroy(cusat_nms_trainer* tr);
+/* out[0..5] = n_ldpc, k_ldpc, n_iter, max_batch, smallest and largest check degree */
+int cusat_nms_trainer_info(const cusat_nms_trainer* tr, int32_t* out);
+/* batch frames of int16 LLRs (device, n_ldpc each, as the decoder takes them)
+ * and their transmitted codewords (device, n_ldpc/8 bytes, MSB first);
+ * theta_dev [n_iter][32][2] = {beta, alpha} (float, device).  Adds the sum
+ * over frames of the loss to *loss_dev and, unless grad_dev is NULL, of its
+ * gradient to grad_dev [n_iter][32][2].  Asynchronous on `stream`. */
+int cusat_nms_train_step(cusat_nms_trainer* tr, const int16_t* llr_dev, const uint8_t* cw_dev, int batch,
+                         const float* theta_dev, float* grad_dev, float* loss_dev, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* Decoding without device allocation                                      */

@@ -37,6 +37,7 @@ def build_oracle(verbose=False):
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "libfec_oracle.so")
     deps = [os.path.join(HERE, "fec_oracle.c"), os.path.join(HERE, "fec_oracle.h"),
+            os.path.join(HERE, "nms_model.inc"),
             os.path.join(HERE, "..", "cusat_gb300", "csrc", "cusat_data.h"),
             os.path.join(HERE, "..", "cusat_gb300", "csrc", "gen", "code_tables.inc")]
     if _newer(out, deps):

@@ -752,3 +752,28 @@ int orc_map(const uint8_t* cw, int B, int cw_bytes, int xfec, int n_mod, const u
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Unrolled learned min-sum (training model), float and double copies       */
+/* ------------------------------------------------------------------------ */
+
+/* Largest number of edges of a check (two parity edges + circulants). */
+static int nms_edge_width(const orc_code* c)
+{
+    int w = 0;
+    for (int i = 0; i < c->q; i++)
+        if (c->lay_off[i + 1] - c->lay_off[i] + 2 > w)
+            w = c->lay_off[i + 1] - c->lay_off[i] + 2;
+    return w;
+}
+
+#define REAL float
+#define SFX(n) n##_f32
+#include "nms_model.inc"
+#undef REAL
+#undef SFX
+#define REAL double
+#define SFX(n) n##_f64
+#include "nms_model.inc"
+#undef REAL
+#undef SFX

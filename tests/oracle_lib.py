@@ -146,3 +146,21 @@ def bnl_update(raw, old):
     d = np.zeros(1, np.int32)
     m = lib().orc_bnl_update(raw, old, _p(d, ctypes.c_int32))
     return m, int(d[0])
+
+
+def nms_train(fs, rate, llr, cw, T, theta, grad=True, dtype=np.float32, nthreads=8):
+    """Loss and gradient (sums over frames) of the unrolled learned min-sum
+    model; theta [T, 32, 2] = {beta, alpha}.  dtype float32 or float64."""
+    info = code_info(fs, rate)
+    llr = np.ascontiguousarray(llr, np.int16).reshape(-1, info["N"])
+    cw = np.ascontiguousarray(cw, np.uint8).reshape(-1, info["N"] // 8)
+    assert llr.shape[0] == cw.shape[0]
+    ct = ctypes.c_float if dtype == np.float32 else ctypes.c_double
+    fn = lib().orc_nms_train_f32 if dtype == np.float32 else lib().orc_nms_train_f64
+    th = np.ascontiguousarray(theta, dtype).reshape(T, 32, 2)
+    g = np.zeros((T, 32, 2), dtype)
+    loss = np.zeros(1, dtype)
+    rc = fn(fs, rate, _p(llr, ctypes.c_int16), _p(cw, ctypes.c_uint8), llr.shape[0], T, _p(th, ct),
+            _p(g, ct) if grad else None, _p(loss, ct), nthreads)
+    assert rc == 0
+    return float(loss[0]), g

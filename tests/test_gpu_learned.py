@@ -1,0 +1,105 @@
+"""Learned min-sum training kernels against the oracle's FP32 model.
+
+The GPU forward/backward (cusat_nms_train_step) and the oracle's
+orc_nms_train_f32 evaluate the same unrolled model; they differ only in the
+order of floating-point additions (atomics on the GPU) and in expf/log1pf
+rounding, so losses and gradients agree to a relative 1e-3.  The oracle's
+analytic backward itself is checked against finite differences in
+test_oracle_nms.py."""
+import numpy as np
+import pytest
+
+import cusat_gb300 as cs
+import oracle_lib as O
+from channel import frames
+from cusat_gb300 import enums as E
+from cusat_gb300 import learned
+from test_gpu_parity import oracle_llr
+
+pytestmark = pytest.mark.gpu
+
+NORMAL, SHORT = E.FECFRAME_NORMAL, E.FECFRAME_SHORT
+
+
+def random_theta(T, seed):
+    rng = np.random.default_rng(seed)
+    th = np.zeros((T, 32, 2), np.float32)
+    th[:, :, 0] = rng.uniform(0.0, 2.0, (T, 32))
+    th[:, :, 1] = rng.uniform(0.55, 1.05, (T, 32))
+    return th
+
+
+def gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, with_grad=True):
+    B = llr.shape[0]
+    tr = learned.nms_trainer(fs, rate, T, B)
+    d_llr = torch.from_numpy(np.ascontiguousarray(llr)).cuda()
+    d_cw = torch.from_numpy(np.ascontiguousarray(cw)).cuda()
+    th = torch.from_numpy(theta).cuda()
+    g = torch.zeros_like(th) if with_grad else None
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    tr.step(d_llr, d_cw, B, th, g, loss, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    return float(loss.item()), (g.cpu().numpy() if with_grad else None), tr
+
+
+@pytest.mark.parametrize("name,fs,esn0,B,T", [("qpsk1/2", SHORT, 0.8, 3, 4), ("8psk3/5", NORMAL, 5.4, 2, 3),
+                                              ("16apsk3/4", NORMAL, 10.2, 2, 3), ("qpsk1/3", NORMAL, 0.3, 2, 3)])
+def test_gradients_match_oracle(cuda, name, fs, esn0, B, T):
+    torch = cuda
+    _, mod, rate, _, _, _ = E.find_modcod(name)
+    _, cw, noisy, n0, gain = frames(mod, rate, fs, B, esn0, seed=21)
+    llr = oracle_llr(mod, rate, fs, noisy, n0, gain)
+    theta = random_theta(T, rate)
+    lg, gg, tr = gpu_loss_grad(torch, fs, rate, llr, cw, T, theta)
+    lc, gc = O.nms_train(fs, rate, llr, cw, T, theta, dtype=np.float32, nthreads=16)
+    assert abs(lg - lc) <= 1e-3 * abs(lc)  # the oracle sums the loss sequentially in float
+    scale = np.abs(gc).max()
+    assert scale > 0
+    assert np.allclose(gg, gc, rtol=1e-3, atol=1e-3 * scale), np.abs(gg - gc).max() / scale
+    # only the code's check degrees carry gradient
+    deg = np.nonzero(np.abs(gc).sum(axis=(0, 2)))[0]
+    assert deg.min() >= tr.deg_lo and deg.max() <= tr.deg_hi
+    # forward only: same loss
+    lf, _, _ = gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, with_grad=False)
+    assert abs(lf - lg) <= 1e-6 * abs(lg)
+
+
+def test_plain_theta_is_exact(cuda):
+    """With beta 1, alpha 1 every value of the model is an integer below 2^24:
+    GPU and oracle follow the same trajectory exactly, so the gradients
+    differ only by the order of their float sums."""
+    torch = cuda
+    fs, rate, T, B = SHORT, E.RATE_1_2, 6, 4
+    _, cw, noisy, n0, gain = frames(E.MOD_QPSK, rate, fs, B, 1.0, seed=4)
+    llr = oracle_llr(E.MOD_QPSK, rate, fs, noisy, n0, gain)
+    theta = learned.plain_theta(T)
+    lg, gg, _ = gpu_loss_grad(torch, fs, rate, llr, cw, T, theta)
+    lc, gc = O.nms_train(fs, rate, llr, cw, T, theta, dtype=np.float32)
+    assert abs(lg - lc) <= 1e-3 * abs(lc)
+    assert np.allclose(gg, gc, rtol=1e-4, atol=1e-5 * np.abs(gc).max())
+
+
+def test_training_lowers_loss_and_quantises(cuda):
+    """A short training run on the GPU lowers the model's loss on held-out
+    frames; the quantised table drives the integer decoder."""
+    torch = cuda
+    name, fs, T = "qpsk1/2", SHORT, 10
+    theta, hist = learned.train(name, fs, n_iter=T, n_frames=64 * 40, batch=64, lr=0.03, seed=3, log=None)
+    assert theta.shape == (T, 32, 2)
+    pool = learned.ChannelPool(name, fs, 64, 99, 64, torch)
+    tr = learned.nms_trainer(fs, pool.rate, T, 64)
+    thr = E.find_modcod(name)[5]
+    losses = {}
+    for key, th in (("plain", learned.plain_theta(T)), ("learned", theta)):
+        d_th = torch.from_numpy(np.ascontiguousarray(th, np.float32)).cuda()
+        loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+        pool.gen.manual_seed(5)
+        for k in range(4):
+            _, llr, cw, _, _ = pool.draw(64, thr + 0.25 * k - 0.25)
+            tr.step(llr, cw, 64, d_th, None, loss)
+        losses[key] = float(loss.item())
+    assert losses["learned"] < losses["plain"], losses
+    w = learned.quantize(theta)
+    assert w.dtype == np.int16 and (w[..., 1] >= 1).all()
+    res = learned.frame_errors(name, fs, thr + 0.5, T, w, n_frames=512, batch=128)
+    assert res["frames"] == 512 and 0 <= res["fer"] <= 1
