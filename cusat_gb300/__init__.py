@@ -27,7 +27,7 @@ from ._capi import CusatError
 from .enums import *  # noqa: F401,F403
 from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
 
-__all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch",
+__all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch", "server",
            "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
            "CusatError", "library_path"]
 
@@ -399,3 +399,62 @@ class batch:
 
     def replay(self, stream):
         _capi.check(_capi.lib().cusat_batch_replay(self._h, _stream(stream)))
+
+
+class server:
+    """Serving loop (continuous batching, HBM-budget admission) over the
+    mixed-MODCOD decoder; see cusat_server_create in include/cusat_fec.h."""
+
+    HOST_SYMBOLS = 1
+
+    def __init__(self, modcods, max_trials=50, hbm_budget=1 << 30, slots=4, max_batch=512):
+        arr = np.ascontiguousarray(np.asarray(modcods, np.int32).reshape(-1, 3))
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_server_create(arr.ctypes.data, arr.shape[0], max_trials, int(hbm_budget),
+                                                    slots, max_batch, ctypes.byref(h)))
+        self._h = h
+        self.modcods = [tuple(int(v) for v in r) for r in arr]
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_server_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def now(self):
+        return float(_capi.lib().cusat_server_now(self._h))
+
+    def set_weights(self, modcod, weights):
+        p, n, _keep = _weights_arg(weights)
+        _capi.check(_capi.lib().cusat_server_set_weights(self._h, modcod, p, n))
+
+    @staticmethod
+    def requests(modcod, noise_var, llr_gain, sym, tag, arrival_s=None, hard_host=None, flags=0):
+        """Array of cusat_request from per-request lists (addresses or tensors)."""
+        n = len(modcod)
+        arr = (_capi.Request * n)()
+        for i in range(n):
+            arr[i] = _capi.Request(int(modcod[i]), float(noise_var[i]), float(llr_gain[i]), flags, _addr(sym[i]),
+                                   None if hard_host is None else _addr(hard_host[i]), int(tag[i]),
+                                   -1.0 if arrival_s is None else float(arrival_s[i]))
+        return arr
+
+    def submit(self, reqs):
+        self._keep.append(reqs)
+        _capi.check(_capi.lib().cusat_server_submit(self._h, ctypes.addressof(reqs), len(reqs)))
+
+    def poll(self, max_results=4096, wait_ms=10):
+        out = (_capi.Result * max_results)()
+        n = _capi.lib().cusat_server_poll(self._h, ctypes.addressof(out), max_results, wait_ms)
+        if n < 0:
+            _capi.check(n)
+        return [out[i] for i in range(n)]
+
+    def stats(self):
+        out = (ctypes.c_double * 8)()
+        _capi.check(_capi.lib().cusat_server_stats(self._h, out))
+        keys = ["pending", "batches", "frames", "largest_batch", "max_inflight_batches", "peak_bytes",
+                "budget_bytes", "inflight_batches"]
+        return dict(zip(keys, list(out)))

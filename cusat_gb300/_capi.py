@@ -58,6 +58,14 @@ _SIGS = {
     "cusat_rx_fec_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p]),
+    "cusat_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_size_t,
+                                           ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_server_destroy": (None, [ctypes.c_void_p]),
+    "cusat_server_now": (ctypes.c_double, [ctypes.c_void_p]),
+    "cusat_server_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "cusat_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "cusat_nms_trainer_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                  ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_nms_trainer_destroy": (None, [ctypes.c_void_p]),
@@ -93,6 +101,20 @@ class Frame(ctypes.Structure):
     _fields_ = [("modcod", ctypes.c_int32), ("noise_var", ctypes.c_float), ("llr_gain", ctypes.c_float),
                 ("reserved", ctypes.c_int32), ("sym", ctypes.c_void_p), ("hard", ctypes.c_void_p),
                 ("trials", ctypes.c_void_p), ("bch_valid", ctypes.c_void_p)]
+
+
+class Request(ctypes.Structure):
+    """cusat_request of include/cusat_fec.h."""
+    _fields_ = [("modcod", ctypes.c_int32), ("noise_var", ctypes.c_float), ("llr_gain", ctypes.c_float),
+                ("flags", ctypes.c_int32), ("sym", ctypes.c_void_p), ("hard_host", ctypes.c_void_p),
+                ("tag", ctypes.c_uint64), ("arrival_s", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    """cusat_result of include/cusat_fec.h."""
+    _fields_ = [("tag", ctypes.c_uint64), ("modcod", ctypes.c_int32), ("trials", ctypes.c_int32),
+                ("bch_valid", ctypes.c_int32), ("reserved", ctypes.c_int32), ("arrival_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double)]
 
 
 class CusatError(RuntimeError):

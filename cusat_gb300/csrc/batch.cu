@@ -268,7 +268,7 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
             rc = fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel fits this MODCOD");
             break;
         }
-        cudaError_t e = cudaFuncSetAttribute(c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, c.proto.sm_total);
+        cudaError_t e = allow_full_smem(c.fn);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sm, c.fn, c.threads, c.proto.sm_total);
         c.grid_max = c.per_sm * b->sms;

@@ -73,8 +73,7 @@ struct Engine {
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
         if (proto.sm_total > optin)
             return fail(CUSAT_ERR_UNSUPPORTED, "frame state does not fit in shared memory");
-        CU(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, proto.sm_total),
-           "cudaFuncSetAttribute");
+        CU(allow_full_smem(fn), "cudaFuncSetAttribute");
         int per_sm = 0;
         CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, proto.sm_total),
            "occupancy");

@@ -45,6 +45,21 @@ inline int require_device(int* dev)
     return CUSAT_OK;
 }
 
+// The dynamic shared-memory cap is a property of the kernel function shared
+// by every object that launches it: objects raise it to the device's opt-in
+// limit and never lower it, so one object's setting cannot make another's
+// larger launch invalid.
+inline cudaError_t allow_full_smem(const void* fn)
+{
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    return e;
+}
+
 // Learned min-sum weights: validates n_iter rows of [32][2] {beta, alpha in
 // 64ths} and expands them to `rows` rows (later rows repeat the last one).
 inline int weight_table(const int16_t* w, int n_iter, int rows, std::vector<int16_t>* out)

@@ -182,7 +182,9 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     const void* fn = cusat::select_decoder_kernel(p->cmax, p->lanes, false);
     if (!fn)
         return fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel for this check degree");
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm_total);
+    // the cap is shared by every object launching this kernel: raise it to
+    // the device limit, never lower it
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, st.optin);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaFuncSetAttribute");
     int per_sm = 0;

@@ -197,3 +197,17 @@ def test_batch_rejects_bad_frames(mixed):
         b.replay(torch.cuda.current_stream())  # nothing captured
     with pytest.raises(cs.CusatError):
         cs.batch([(E.MOD_QPSK, E.RATE_1_2, 7)])
+
+
+def test_single_code_objects_created_later_leave_the_batch_launchable(mixed):
+    """A single-MODCOD object of the same kernel class needs less shared
+    memory than the batch; creating one after the batch must not lower what
+    the batch may launch with."""
+    torch, per, T, ref, order = mixed
+    b = cs.batch(_modcod_triples(per), max_trials=T, max_frames=64)
+    keep = [cs.rx_fec(mod, rate, fs, T, 1) for mod, rate, fs in _modcod_triples(per)]
+    keep += [cs.ldpc_decode_cuda(fs, rate, T, 1) for _, rate, fs in _modcod_triples(per)]
+    bufs, frames = _buffers(per, order, torch)
+    b.launch(frames, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    _check(bufs, ref)
