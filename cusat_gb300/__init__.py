@@ -401,6 +401,16 @@ class batch:
         _capi.check(_capi.lib().cusat_batch_replay(self._h, _stream(stream)))
 
 
+# cusat_result as a numpy record (48 bytes, the C layout)
+_RESULT = np.dtype([("tag", "<u8"), ("modcod", "<i4"), ("trials", "<i4"), ("bch_valid", "<i4"), ("reserved", "<i4"),
+                    ("arrival_s", "<f8"), ("admit_s", "<f8"), ("done_s", "<f8")])
+
+
+import collections as _collections  # noqa: E402
+
+ServerResult = _collections.namedtuple("ServerResult", list(_RESULT.names))
+
+
 class server:
     """Serving loop (continuous batching, HBM-budget admission) over the
     mixed-MODCOD decoder; see cusat_server_create in include/cusat_fec.h."""
@@ -446,11 +456,13 @@ class server:
         _capi.check(_capi.lib().cusat_server_submit(self._h, ctypes.addressof(reqs), len(reqs)))
 
     def poll(self, max_results=4096, wait_ms=10):
+        """Completed results (namedtuples with the cusat_result fields)."""
         out = (_capi.Result * max_results)()
         n = _capi.lib().cusat_server_poll(self._h, ctypes.addressof(out), max_results, wait_ms)
         if n < 0:
             _capi.check(n)
-        return [out[i] for i in range(n)]
+        rec = np.frombuffer(out, dtype=_RESULT, count=n)
+        return [ServerResult(*r) for r in rec.tolist()]
 
     def stats(self):
         out = (ctypes.c_double * 8)()

@@ -14,7 +14,8 @@
 //       other edges, (beta, alpha) = theta[t][deg(c)]
 //   then every touched L[v] += m - m_old (additive within a step, like the
 //   integer decoder's shared groups).
-//   loss = (1/T) sum_t (1/N) sum_v softplus(-y_v L_v after iteration t).
+//   loss = sum_t w_t (1/N) sum_v softplus(-y_v L_v after iteration t), w_t
+//   the per-iteration loss weights (1/T each by default).
 //
 // L and dL/dL are updated with atomics (L2) and read back with L1-bypassing
 // loads after each barrier.
@@ -55,6 +56,7 @@ struct TrainArgs {
     const int16_t* llr;  // [B][N]
     const uint8_t* cw;   // [B][N/8] transmitted codewords, MSB first
     const float* theta;  // [T][32][2] {beta, alpha}
+    const float* iter_w; // [T] loss weight per iteration, or nullptr (1/T)
     float* grad;         // [T][32][2] accumulated, or nullptr (forward only)
     float* loss;         // [1] accumulated
     float* L;            // [grid][N]
@@ -135,7 +137,8 @@ __global__ void __launch_bounds__(2 * kTrainLane, 1) nms_train_kernel(TrainArgs 
     const int lane = tid / kTrainLane;
     const int j = tid - lane * kTrainLane;
     const int N = c.N, R = c.R, EW = c.ew, T = a.T;
-    const float w = 1.0f / ((float)T * (float)N);
+    const float inv_n = 1.0f / (float)N;
+    auto wt = [&](int t) { return (a.iter_w ? a.iter_w[t] : 1.0f / (float)T) * inv_n; };
     float* L = a.L + (size_t)blockIdx.x * N;
     float* gL = a.gL + (size_t)blockIdx.x * N;
     float* G = a.G + (size_t)blockIdx.x * R * EW;
@@ -205,13 +208,14 @@ __global__ void __launch_bounds__(2 * kTrainLane, 1) nms_train_kernel(TrainArgs 
                 }
                 __syncthreads();
             }
-            for (int v = tid; v < N; v += blockDim.x)
-                {
+            float lt = 0.0f;
+            for (int v = tid; v < N; v += blockDim.x) {
                 const float l = __ldcg(&L[v]);
-                loss += softplus_of(code_bit(cw, v) ? l : -l);
+                lt += softplus_of(code_bit(cw, v) ? l : -l);
             }
+            loss += wt(t) * lt;
         }
-        loss = warp_sum(loss * w);
+        loss = warp_sum(loss);
         if ((tid & 31) == 0)
             s_red[tid >> 5] = loss;
         __syncthreads();
@@ -228,7 +232,7 @@ __global__ void __launch_bounds__(2 * kTrainLane, 1) nms_train_kernel(TrainArgs 
 
         // ---------------- backward ----------------
         for (int v = tid; v < N; v += blockDim.x)
-            gL[v] = w * dsoftplus_of(__ldcg(&L[v]), code_bit(cw, v));
+            gL[v] = wt(T - 1) * dsoftplus_of(__ldcg(&L[v]), code_bit(cw, v));
         for (int k = tid; k < R * EW; k += blockDim.x)
             G[k] = 0.0f;
         __syncthreads();
@@ -314,7 +318,7 @@ __global__ void __launch_bounds__(2 * kTrainLane, 1) nms_train_kernel(TrainArgs 
             }
             if (t > 0)
                 for (int v = tid; v < N; v += blockDim.x)
-                    gL[v] = __ldcg(&gL[v]) + w * dsoftplus_of(__ldcg(&L[v]), code_bit(cw, v));
+                    gL[v] = __ldcg(&gL[v]) + wt(t - 1) * dsoftplus_of(__ldcg(&L[v]), code_bit(cw, v));
             if (tid < 64) {
                 const float g = s_g[tid];
                 if (g != 0.0f)
@@ -450,7 +454,8 @@ int cusat_nms_trainer_info(const cusat_nms_trainer* t, int32_t* out)
 }
 
 int cusat_nms_train_step(cusat_nms_trainer* t, const int16_t* llr_dev, const uint8_t* cw_dev, int batch,
-                         const float* theta_dev, float* grad_dev, float* loss_dev, void* stream)
+                         const float* theta_dev, const float* iter_w_dev, float* grad_dev, float* loss_dev,
+                         void* stream)
 {
     if (!t || !llr_dev || !cw_dev || !theta_dev || !loss_dev || batch <= 0 || batch > t->max_batch)
         return fail(CUSAT_ERR_ARG, "invalid training step arguments");
@@ -459,6 +464,7 @@ int cusat_nms_train_step(cusat_nms_trainer* t, const int16_t* llr_dev, const uin
     a.llr = llr_dev;
     a.cw = cw_dev;
     a.theta = theta_dev;
+    a.iter_w = iter_w_dev;
     a.grad = grad_dev;
     a.loss = loss_dev;
     const int grid = std::min(batch, t->grid);

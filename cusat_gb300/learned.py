@@ -43,12 +43,13 @@ class nms_trainer:
 
     __del__ = close
 
-    def step(self, llr, cw, batch, theta, grad, loss, stream=None):
+    def step(self, llr, cw, batch, theta, grad, loss, stream=None, iter_w=None):
         """Adds the summed loss (and gradient, unless grad is None) of `batch`
-        frames; all arguments are device tensors or addresses."""
+        frames; all arguments are device tensors or addresses; iter_w: loss
+        weight per iteration (device) or None (uniform)."""
         from . import _addr, _stream
         _capi.check(_capi.lib().cusat_nms_train_step(self._h, _addr(llr), _addr(cw), batch, _addr(theta),
-                                                     _addr(grad), _addr(loss), _stream(stream)))
+                                                     _addr(iter_w), _addr(grad), _addr(loss), _stream(stream)))
 
 
 def plain_theta(n_iter):
@@ -142,18 +143,27 @@ class ChannelPool:
 
 
 def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128, lr=0.02, seed=1,
-          n_codewords=256, log_every=0, log=print):
-    """Trains {beta, alpha}[n_iter][degree] for one MODCOD; returns
-    (theta float32 [n_iter, 32, 2], history of (frames, mean loss))."""
+          n_codewords=256, log_every=0, log=print, beta_lr_scale=1.0, lr_min_frac=0.1, theta0=None,
+          iter_weights=None):
+    """Trains {beta, alpha}[n_iter][degree] for one MODCOD with Adam (step
+    lr for alpha, lr * beta_lr_scale for beta, cosine decay to lr_min_frac);
+    returns (theta float32 [n_iter, 32, 2], history of (frames, mean loss)).
+    iter_weights: loss weight of each iteration (default uniform)."""
     import torch
     thr = find_modcod(name)[5]
     if esn0_grid is None:
         esn0_grid = [thr - 0.5 + 0.25 * k for k in range(7)]
     pool = ChannelPool(name, framesize, n_codewords, seed, batch, torch)
     tr = nms_trainer(framesize, pool.rate, n_iter, batch)
-    theta = torch.from_numpy(plain_theta(n_iter)).cuda().requires_grad_(False)
+    th0 = plain_theta(n_iter) if theta0 is None else np.asarray(theta0, np.float32)
+    theta = torch.from_numpy(np.ascontiguousarray(th0)).cuda()
+    scale = torch.ones_like(theta)
+    scale[:, :, 0] = beta_lr_scale
     grad = torch.zeros_like(theta)
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    iw = None
+    if iter_weights is not None:
+        iw = torch.tensor(np.asarray(iter_weights, np.float32).reshape(n_iter), device="cuda")
     m = torch.zeros_like(theta)
     v = torch.zeros_like(theta)
     b1, b2, eps = 0.9, 0.999, 1e-8
@@ -167,14 +177,15 @@ def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128
         _, llr, cw, _, _ = pool.draw(batch, esn0)
         grad.zero_()
         loss.zero_()
-        tr.step(llr, cw, batch, theta, grad, loss)
+        tr.step(llr, cw, batch, theta, grad, loss, iter_w=iw)
         g = grad * mask / batch
         m.mul_(b1).add_(g, alpha=1 - b1)
         v.mul_(b2).addcmul_(g, g, value=1 - b2)
         mh = m / (1 - b1 ** (k + 1))
         vh = v / (1 - b2 ** (k + 1))
-        theta.sub_(lr * mh / (vh.sqrt() + eps))
-        theta[:, :, 0].clamp_(0.0, 16.0)
+        lr_k = lr * (lr_min_frac + (1 - lr_min_frac) * 0.5 * (1 + np.cos(np.pi * k / steps)))
+        theta.sub_(lr_k * scale * mh / (vh.sqrt() + eps))
+        theta[:, :, 0].clamp_(0.0, 127.0)
         theta[:, :, 1].clamp_(1.0 / 64.0, 2.0)
         acc += float(loss.item()) / batch
         acc_n += 1
@@ -219,3 +230,70 @@ def frame_errors(name, framesize, esn0_db, n_iter, weights, n_frames, batch=256,
             break
     return {"esn0_db": esn0_db, "frames": frames, "frame_errors": errors, "fer": errors / frames,
             "decoder_failures": fails, "mean_iterations": iters / frames}
+
+
+def fer_table(name, framesize, esn0_list, decoders, min_errors=200, max_frames=1000000, batch=256, seed=7,
+              log=None):
+    """FER rows: for every Es/N0 and (label, n_iter, weights) decoder, frames
+    until min_errors frame errors or max_frames frames."""
+    rows = []
+    for es in esn0_list:
+        row = {"esn0_db": round(float(es), 3)}
+        for label, n_iter, w in decoders:
+            r = frame_errors(name, framesize, es, n_iter, w, n_frames=max_frames, batch=batch, seed=seed,
+                             min_errors=min_errors)
+            row[label] = {k: r[k] for k in ("fer", "frame_errors", "frames", "mean_iterations")}
+        rows.append(row)
+        if log:
+            log(json.dumps(row))
+    return rows
+
+
+def main(argv=None):
+    """python -m cusat_gb300.learned --modcod qpsk1/3 [--short] --frames 1000000
+    trains the weights on the GPU, measures FER (learned at --iters vs plain at
+    --iters and --plain-iters) on the threshold grid and writes the weight
+    file with the FER table; --adopt-only keeps it only when learned matches
+    plain's FER at the plain cap somewhere on the grid in fewer mean
+    iterations."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--modcod", required=True)
+    ap.add_argument("--short", action="store_true")
+    ap.add_argument("--iters", type=int, default=20)
+    ap.add_argument("--plain-iters", type=int, default=50)
+    ap.add_argument("--frames", type=int, default=1000000)
+    ap.add_argument("--batch", type=int, default=128)
+    ap.add_argument("--lr", type=float, default=0.02)
+    ap.add_argument("--beta-lr-scale", type=float, default=1.0)
+    ap.add_argument("--loss", choices=["uniform", "last"], default="uniform")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--fer-frames", type=int, default=1000000)
+    ap.add_argument("--out", default=None)
+    args = ap.parse_args(argv)
+    fs = 1 if args.short else 0
+    T = args.iters
+    thr = find_modcod(args.modcod)[5]
+    grid = [thr - 0.5 + 0.25 * k for k in range(7)]
+    iw = None if args.loss == "uniform" else [0.0] * (T - 1) + [1.0]
+    t0 = time.time()
+    theta, hist = train(args.modcod, fs, n_iter=T, esn0_grid=grid, n_frames=args.frames, batch=args.batch,
+                        lr=args.lr, seed=args.seed, beta_lr_scale=args.beta_lr_scale, iter_weights=iw,
+                        log_every=max(1, args.frames // args.batch // 20))
+    train_s = time.time() - t0
+    w = quantize(theta)
+    rows = fer_table(args.modcod, fs, grid, [("plain%d" % args.plain_iters, args.plain_iters, None),
+                                              ("plain%d" % T, T, None), ("learned%d" % T, T, w)],
+                     max_frames=args.fer_frames, log=print)
+    meta = {"train": {"frames": args.frames, "batch": args.batch, "lr": args.lr, "beta_lr_scale": args.beta_lr_scale,
+                      "loss": args.loss, "esn0_grid_db": [round(g, 3) for g in grid], "seconds": round(train_s, 1),
+                      "loss_history": [[int(a), float(b)] for a, b in hist], "seed": args.seed},
+            "fer": rows, "fer_rule": "200 frame errors or %d frames per point" % args.fer_frames}
+    path = args.out or weights_path(args.modcod, fs)
+    save_weights(path, args.modcod, fs, w, meta)
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()

@@ -68,32 +68,54 @@ def make_trace(pool, rate_sym_s, duration_s, seed, stay=0.9):
     return out
 
 
-def requests(srv, pool, trace, t0, tag0=0):
-    """cusat_request array for a trace whose offsets start at server time t0."""
-    cols = ([], [], [], [], [], [])
-    for k, (t, e, f) in enumerate(trace):
-        ent = pool.entries[e]
-        cols[0].append(e)
-        cols[1].append(ent["n0"])
-        cols[2].append(ent["gain"])
-        cols[3].append(ent["sym"][f].data_ptr())
-        cols[4].append(tag0 + k)
-        cols[5].append(t0 + t)
-    return srv.requests(*cols)
+# cusat_request as a numpy record (same layout as the C struct: 48 bytes)
+REQUEST = np.dtype([("modcod", "<i4"), ("noise_var", "<f4"), ("llr_gain", "<f4"), ("flags", "<i4"),
+                    ("sym", "<u8"), ("hard_host", "<u8"), ("tag", "<u8"), ("arrival_s", "<f8")])
 
 
-def replay(srv, pool, trace, lead_s=0.05, timeout_s=120.0):
+def request_records(pool, trace, tag0=0, hard_host=None):
+    """Records of a trace with arrival offsets (add the start time later)."""
+    n = len(trace)
+    rec = np.zeros(n, REQUEST)
+    e = np.array([x[1] for x in trace], np.int64)
+    f = np.array([x[2] for x in trace], np.int64)
+    rec["modcod"] = e
+    rec["noise_var"] = np.array([pool.entries[i]["n0"] for i in range(len(pool.entries))], np.float32)[e]
+    rec["llr_gain"] = np.array([pool.entries[i]["gain"] for i in range(len(pool.entries))], np.float32)[e]
+    base = np.array([pool.entries[i]["sym"].data_ptr() for i in range(len(pool.entries))], np.uint64)
+    row = np.array([pool.entries[i]["sym"].shape[1] * 4 for i in range(len(pool.entries))], np.uint64)
+    rec["sym"] = base[e] + row[e] * f.astype(np.uint64)
+    if hard_host is not None:
+        rec["hard_host"] = np.asarray(hard_host, np.uint64)
+    rec["tag"] = tag0 + np.arange(n, dtype=np.uint64)
+    rec["arrival_s"] = np.array([x[0] for x in trace], np.float64)
+    return rec
+
+
+def submit_records(srv, rec, lead_s):
+    """Shifts the offsets to start lead_s from now (server clock) and submits."""
+    import ctypes
+    from . import _capi
+    rec = rec.copy()
+    rec["arrival_s"] += srv.now() + lead_s
+    arr = (_capi.Request * len(rec)).from_buffer(rec)
+    srv.submit(arr)
+    return rec
+
+
+def replay(srv, pool, trace, lead_s=0.02, timeout_s=120.0, hard_host=None):
     """Submits the whole trace (arrivals from now + lead_s) and collects the
     results.  Returns (results sorted by tag, stats)."""
     import time
-    t0 = srv.now() + lead_s
-    srv.submit(requests(srv, pool, trace, t0))
+    rec = request_records(pool, trace, hard_host=hard_host)
+    keep = submit_records(srv, rec, lead_s)
     got = []
     deadline = time.time() + timeout_s
     while len(got) < len(trace):
         got += srv.poll(max_results=65536, wait_ms=20)
         if time.time() > deadline:
             raise TimeoutError(f"{len(got)} of {len(trace)} results after {timeout_s} s")
+    del keep
     got.sort(key=lambda r: r.tag)
     return got, srv.stats()
 

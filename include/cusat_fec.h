@@ -296,20 +296,23 @@ typedef struct cusat_nms_trainer cusat_nms_trainer;
  * decoder with learnable {beta, alpha} per iteration (n_iter <= 64) and
  * check degree: per check, m_e = sign product of the other edges *
  * min(alpha * max(r_e - beta, 0), 127), r_e the smallest |extrinsic| of the
- * other edges; the reference's paired-layer schedule; loss = mean over
- * iterations and bits of softplus(-y L) (y = +1 for a 0 bit, L the APP after
- * the iteration).  Forward and backward run on the GPU, one CTA per frame. */
+ * other edges; the reference's paired-layer schedule; loss = sum over
+ * iterations t of w_t times the mean over bits of softplus(-y L) (y = +1 for
+ * a 0 bit, L the APP after iteration t).  Forward and backward run on the GPU, one CTA per frame. */
 int cusat_nms_trainer_create(int framesize, int rate, int n_iter, int max_batch, cusat_nms_trainer** out);
 void cusat_nms_trainer_destroy(cusat_nms_trainer* tr);
 /* out[0..5] = n_ldpc, k_ldpc, n_iter, max_batch, smallest and largest check degree */
 int cusat_nms_trainer_info(const cusat_nms_trainer* tr, int32_t* out);
 /* batch frames of int16 LLRs (device, n_ldpc each, as the decoder takes them)
  * and their transmitted codewords (device, n_ldpc/8 bytes, MSB first);
- * theta_dev [n_iter][32][2] = {beta, alpha} (float, device).  Adds the sum
+ * theta_dev [n_iter][32][2] = {beta, alpha} (float, device); iter_w_dev
+ * [n_iter] loss weight of each iteration's APP (device, or NULL: 1/n_iter
+ * each).  Adds the sum
  * over frames of the loss to *loss_dev and, unless grad_dev is NULL, of its
  * gradient to grad_dev [n_iter][32][2].  Asynchronous on `stream`. */
 int cusat_nms_train_step(cusat_nms_trainer* tr, const int16_t* llr_dev, const uint8_t* cw_dev, int batch,
-                         const float* theta_dev, float* grad_dev, float* loss_dev, void* stream);
+                         const float* theta_dev, const float* iter_w_dev, float* grad_dev, float* loss_dev,
+                         void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* Decoding without device allocation                                      */

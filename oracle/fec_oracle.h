@@ -82,12 +82,13 @@ float orc_log(float x);
 /* Unrolled learned min-sum (training model; nms_model.inc): loss and its
  * gradient with respect to theta[T][32][2] = {beta, alpha} per iteration and
  * check degree, summed over B frames of int16 LLRs and packed codewords
- * (N/8 bytes, MSB first).  grad (may be NULL) and loss are accumulated into.
- * float and double copies of the same code. */
+ * (N/8 bytes, MSB first).  iter_w: per-iteration loss weights or NULL
+ * (uniform).  grad (may be NULL) and loss are accumulated into.  float and
+ * double copies of the same code. */
 int orc_nms_train_f32(int framesize, int rate, const int16_t* llr, const uint8_t* cw, int B, int T,
-                      const float* theta, float* grad, float* loss, int nthreads);
+                      const float* theta, const float* iter_w, float* grad, float* loss, int nthreads);
 int orc_nms_train_f64(int framesize, int rate, const int16_t* llr, const uint8_t* cw, int B, int T,
-                      const double* theta, double* grad, double* loss, int nthreads);
+                      const double* theta, const double* iter_w, double* grad, double* loss, int nthreads);
 
 #ifdef __cplusplus
 }

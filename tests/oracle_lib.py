@@ -148,9 +148,10 @@ def bnl_update(raw, old):
     return m, int(d[0])
 
 
-def nms_train(fs, rate, llr, cw, T, theta, grad=True, dtype=np.float32, nthreads=8):
+def nms_train(fs, rate, llr, cw, T, theta, grad=True, dtype=np.float32, nthreads=8, iter_w=None):
     """Loss and gradient (sums over frames) of the unrolled learned min-sum
-    model; theta [T, 32, 2] = {beta, alpha}.  dtype float32 or float64."""
+    model; theta [T, 32, 2] = {beta, alpha}; iter_w [T] loss weights or None
+    (uniform).  dtype float32 or float64."""
     info = code_info(fs, rate)
     llr = np.ascontiguousarray(llr, np.int16).reshape(-1, info["N"])
     cw = np.ascontiguousarray(cw, np.uint8).reshape(-1, info["N"] // 8)
@@ -160,7 +161,8 @@ def nms_train(fs, rate, llr, cw, T, theta, grad=True, dtype=np.float32, nthreads
     th = np.ascontiguousarray(theta, dtype).reshape(T, 32, 2)
     g = np.zeros((T, 32, 2), dtype)
     loss = np.zeros(1, dtype)
+    iw = None if iter_w is None else np.ascontiguousarray(iter_w, dtype).reshape(T)
     rc = fn(fs, rate, _p(llr, ctypes.c_int16), _p(cw, ctypes.c_uint8), llr.shape[0], T, _p(th, ct),
-            _p(g, ct) if grad else None, _p(loss, ct), nthreads)
+            None if iw is None else _p(iw, ct), _p(g, ct) if grad else None, _p(loss, ct), nthreads)
     assert rc == 0
     return float(loss[0]), g

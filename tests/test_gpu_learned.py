@@ -29,7 +29,7 @@ def random_theta(T, seed):
     return th
 
 
-def gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, with_grad=True):
+def gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, with_grad=True, iter_w=None):
     B = llr.shape[0]
     tr = learned.nms_trainer(fs, rate, T, B)
     d_llr = torch.from_numpy(np.ascontiguousarray(llr)).cuda()
@@ -37,7 +37,8 @@ def gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, with_grad=True):
     th = torch.from_numpy(theta).cuda()
     g = torch.zeros_like(th) if with_grad else None
     loss = torch.zeros(1, dtype=torch.float32, device="cuda")
-    tr.step(d_llr, d_cw, B, th, g, loss, torch.cuda.current_stream())
+    iw = None if iter_w is None else torch.tensor(np.asarray(iter_w, np.float32), device="cuda")
+    tr.step(d_llr, d_cw, B, th, g, loss, torch.cuda.current_stream(), iter_w=iw)
     torch.cuda.synchronize()
     return float(loss.item()), (g.cpu().numpy() if with_grad else None), tr
 
@@ -62,6 +63,19 @@ def test_gradients_match_oracle(cuda, name, fs, esn0, B, T):
     # forward only: same loss
     lf, _, _ = gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, with_grad=False)
     assert abs(lf - lg) <= 1e-6 * abs(lg)
+
+
+def test_iteration_weights_match_oracle(cuda):
+    torch = cuda
+    fs, rate, T, B = SHORT, E.RATE_1_2, 5, 3
+    _, cw, noisy, n0, gain = frames(E.MOD_QPSK, rate, fs, B, 0.9, seed=9)
+    llr = oracle_llr(E.MOD_QPSK, rate, fs, noisy, n0, gain)
+    theta = random_theta(T, 4)
+    iw = [0.0, 0.05, 0.1, 0.35, 1.0]
+    lg, gg, _ = gpu_loss_grad(torch, fs, rate, llr, cw, T, theta, iter_w=iw)
+    lc, gc = O.nms_train(fs, rate, llr, cw, T, theta, dtype=np.float32, iter_w=iw)
+    assert abs(lg - lc) <= 1e-3 * abs(lc)
+    assert np.allclose(gg, gc, rtol=1e-3, atol=1e-3 * np.abs(gc).max())
 
 
 def test_plain_theta_is_exact(cuda):

@@ -29,13 +29,14 @@ def _theta(T, seed):
     return th
 
 
-@pytest.mark.parametrize("fs,rate,mod,esn0", [(SHORT, E.RATE_1_2, E.MOD_QPSK, 1.0),
-                                              (SHORT, E.RATE_3_5, E.MOD_8PSK, 5.0)])
-def test_backward_matches_finite_differences(fs, rate, mod, esn0):
+@pytest.mark.parametrize("fs,rate,mod,esn0,iw", [(SHORT, E.RATE_1_2, E.MOD_QPSK, 1.0, None),
+                                                 (SHORT, E.RATE_3_5, E.MOD_8PSK, 5.0, None),
+                                                 (SHORT, E.RATE_1_2, E.MOD_QPSK, 1.0, [0.0, 0.1, 0.3, 1.0])])
+def test_backward_matches_finite_differences(fs, rate, mod, esn0, iw):
     llr, cw = _llr(mod, rate, fs, 2, esn0, seed=3)
     T = 4
     th = _theta(T, 0)
-    loss, g = O.nms_train(fs, rate, llr, cw, T, th, dtype=np.float64)
+    loss, g = O.nms_train(fs, rate, llr, cw, T, th, dtype=np.float64, iter_w=iw)
     assert loss > 0
     nz = np.argwhere(g != 0)
     assert len(nz) >= 8
@@ -48,8 +49,8 @@ def test_backward_matches_finite_differences(fs, rate, mod, esn0):
         tp, tm = th.copy(), th.copy()
         tp[t, d, k] += eps
         tm[t, d, k] -= eps
-        lp, _ = O.nms_train(fs, rate, llr, cw, T, tp, grad=False, dtype=np.float64)
-        lm, _ = O.nms_train(fs, rate, llr, cw, T, tm, grad=False, dtype=np.float64)
+        lp, _ = O.nms_train(fs, rate, llr, cw, T, tp, grad=False, dtype=np.float64, iter_w=iw)
+        lm, _ = O.nms_train(fs, rate, llr, cw, T, tm, grad=False, dtype=np.float64, iter_w=iw)
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - g[t, d, k]) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(g).max()), (t, d, k, fd, g[t, d, k])
 
@@ -93,3 +94,24 @@ def test_noiseless_frames_have_small_loss():
     loss, g = O.nms_train(fs, rate, llr, cw, 3, _theta(3, 1), dtype=np.float64)
     assert loss < 1e-20
     assert np.abs(g).max() < 1e-20
+
+
+def test_iteration_weights_are_linear():
+    """The loss is linear in the iteration weights: uniform weights equal the
+    default, and a weight vector's loss is the weighted sum of one-hot ones."""
+    llr, cw = _llr(E.MOD_QPSK, E.RATE_1_2, SHORT, 2, 1.2, seed=5)
+    T = 3
+    th = _theta(T, 6)
+    l0, g0 = O.nms_train(SHORT, E.RATE_1_2, llr, cw, T, th, dtype=np.float64)
+    lu, gu = O.nms_train(SHORT, E.RATE_1_2, llr, cw, T, th, dtype=np.float64, iter_w=[1 / T] * T)
+    assert abs(l0 - lu) <= 1e-12 * l0 and np.allclose(g0, gu, rtol=1e-10, atol=1e-16)
+    w = np.array([0.2, 0.5, 1.5])
+    lw, gw = O.nms_train(SHORT, E.RATE_1_2, llr, cw, T, th, dtype=np.float64, iter_w=w)
+    ls, gs = 0.0, np.zeros_like(gw)
+    for t in range(T):
+        e = np.zeros(T)
+        e[t] = w[t]
+        lt, gt = O.nms_train(SHORT, E.RATE_1_2, llr, cw, T, th, dtype=np.float64, iter_w=e)
+        ls += lt
+        gs += gt
+    assert abs(lw - ls) <= 1e-10 * lw and np.allclose(gw, gs, rtol=1e-9, atol=1e-15)
