@@ -57,9 +57,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames in the CPU sample (0 = auto)")
-    ap.add_argument("--workload", choices=["single", "mixed", "serve"], default="single",
+    ap.add_argument("--workload", choices=["single", "mixed", "serve", "learned"], default="single",
                     help="single: the headline 8PSK 3/5 batch; mixed: 1024 frames of 10 MODCODs in a CUDA graph; "
-                         "serve: Poisson arrivals through the serving loop")
+                         "serve: Poisson arrivals through the serving loop; learned: plain (max 50 it) vs "
+                         "learned (max 20 it) min-sum on normal QPSK 1/3 at its threshold")
     ap.add_argument("--rates", default="0.5,1,2,3,4,5", help="serve: aggregate Gsym/s to sweep")
     ap.add_argument("--duration", type=float, default=0.25, help="serve: seconds of traffic per rate")
     return ap.parse_args()
@@ -209,8 +210,9 @@ def main():
     import cusat_gb300 as cs
     from cusat_gb300 import build as lib_build
     lib_build.build()
-    if args.workload in ("mixed", "serve"):
-        (mixed_main if args.workload == "mixed" else serve_main)(args, torch, cs, rank, local_rank, world)
+    if args.workload in ("mixed", "serve", "learned"):
+        {"mixed": mixed_main, "serve": serve_main, "learned": learned_main}[args.workload](
+            args, torch, cs, rank, local_rank, world)
         if world > 1:
             torch.distributed.destroy_process_group()
         return
@@ -618,6 +620,82 @@ def serve_main(args, torch, cs, rank, local_rank, world):
                                "batching on 4 slots (max 512 frames per batch), max 50 iterations",
                    "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "rates": rows},
         "clocks": clk,
+    }), flush=True)
+
+
+LEARNED = {"name": "normal 1/3 QPSK", "modcod": "qpsk1/3", "fs": 0, "rate": 1, "mod": 0, "frames": 256,
+           "esn0_db": 0.56, "seed": 2027}
+
+
+def learned_main(args, torch, cs, rank, local_rank, world):
+    """Plain offset min-sum capped at 50 iterations against the learned
+    weights capped at 20, same frames, same timing as the headline (two
+    chains on two streams, inputs cycled over 4 batches); value = learned
+    info Gbit/s.  Frame errors are counted against the sent codewords."""
+    from cusat_gb300 import learned, replicas
+    wl = dict(LEARNED)
+    from cusat_gb300.enums import find_modcod
+    _, wl["mod"], wl["rate"], _, _, _ = find_modcod(wl["modcod"])
+    w = learned.load_weights(wl["modcod"], wl["fs"])
+    if w is None:
+        raise RuntimeError("no adopted weight file for " + wl["modcod"])
+    ci, msg, bufs, n0, gain = make_traffic(wl, N_BUFS)
+    B = wl["frames"]
+    sent = [torch.from_numpy(cs.encode_frames(wl["fs"], wl["rate"], msg)[:, :ci["k_ldpc"] // 8]).cuda()]
+    d_sym = [torch.from_numpy(b).cuda() for b in bufs]
+    streams = [torch.cuda.Stream() for _ in range(PIPE)]
+    res = {}
+    for label, T, wt in (("plain50", 50, None), ("learned20", 20, w)):
+        rxs = [cs.rx_fec(wl["mod"], wl["rate"], wl["fs"], T, B) for _ in range(PIPE)]
+        for rx in rxs:
+            rx.set_weights(wt)
+        outs = [(torch.zeros((B, rxs[0].k_bytes), dtype=torch.uint8, device="cuda"),
+                 torch.zeros(B, dtype=torch.int32, device="cuda")) for _ in range(PIPE)]
+
+        def step(i):
+            k = i % PIPE
+            with torch.cuda.stream(streams[k]):
+                rxs[k].launch(d_sym[i % N_BUFS], B, n0, gain, outs[k][0], outs[k][1], None, streams[k])
+
+        for i in range(args.warmup):
+            step(i)
+        torch.cuda.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        start.record(streams[0])
+        for st in streams[1:]:
+            st.wait_event(start)
+        for i in range(args.steps):
+            step(i)
+        for st in streams[1:]:
+            ev = torch.cuda.Event()
+            ev.record(st)
+            streams[0].wait_event(ev)
+        end = torch.cuda.Event(enable_timing=True)
+        end.record(streams[0])
+        torch.cuda.synchronize()
+        ms = replicas.reduce_timing([start.elapsed_time(end)], device="cuda")[0]
+        errors = frames = iters = 0
+        for i in range(N_BUFS):
+            rxs[0].launch(d_sym[i], B, n0, gain, outs[0][0], outs[0][1], None, streams[0])
+            streams[0].synchronize()
+            errors += int((outs[0][0] != sent[0]).any(dim=1).sum().item())
+            tr = outs[0][1].cpu().numpy()
+            iters += float(np.sum(np.where(tr >= 0, T - tr, T)))
+            frames += B
+        res[label] = {"gbit_s": args.steps * B * ci["k_ldpc"] * world / (ms * 1e-3) / 1e9,
+                      "ms_per_step": ms / args.steps, "frame_errors": errors, "frames": frames,
+                      "mean_iterations": iters / frames}
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": METRIC, "value": res["learned20"]["gbit_s"], "unit": "Gbit/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["learned20"]["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
+        "data": "synthetic (seeded BCH/LDPC-encoded QPSK frames, AWGN at Es/N0 0.56 dB)",
+        "config": {"workload": "normal 1/3 QPSK (s2_b2), 256 frames at its threshold 0.56 dB: fused demap -> "
+                               "learned min-sum (max 20 it) vs plain (max 50 it) -> BCH",
+                   "learned": res["learned20"], "plain": res["plain50"],
+                   "speedup": res["learned20"]["gbit_s"] / res["plain50"]["gbit_s"]},
     }), flush=True)
 
 

@@ -90,14 +90,29 @@ def save_weights(path, name, framesize, w, meta):
         json.dump(doc, f, indent=1)
 
 
-def load_weights(name, framesize, path=None):
-    """The stored int16 table [n_iter, 32, 2], or None (decode plain)."""
+def load_weights(name, framesize, path=None, adopted_only=True):
+    """The stored int16 table [n_iter, 32, 2], or None (decode plain): a
+    weight file that was not adopted (its learned FER lost to the plain
+    decoder somewhere on its grid) is ignored unless adopted_only is False."""
     path = path or weights_path(name, framesize)
     if not os.path.exists(path):
         return None
     with open(path) as f:
         doc = json.load(f)
+    if adopted_only and not doc.get("meta", {}).get("adopted", False):
+        return None
     return np.asarray(doc["weights"], np.int16)
+
+
+def adopted(rows, learned_key, plain_key):
+    """True when, at every Es/N0 of the table, the learned decoder's frame
+    errors do not exceed the plain decoder's by more than chance: learned
+    FER <= 1.5 x plain FER + 3 / frames."""
+    for r in rows:
+        a, b = r[learned_key], r[plain_key]
+        if a["fer"] > 1.5 * b["fer"] + 3.0 / max(a["frames"], 1):
+            return False
+    return True
 
 
 class ChannelPool:
@@ -253,9 +268,9 @@ def main(argv=None):
     """python -m cusat_gb300.learned --modcod qpsk1/3 [--short] --frames 1000000
     trains the weights on the GPU, measures FER (learned at --iters vs plain at
     --iters and --plain-iters) on the threshold grid and writes the weight
-    file with the FER table; --adopt-only keeps it only when learned matches
-    plain's FER at the plain cap somewhere on the grid in fewer mean
-    iterations."""
+    file with the FER table, marked adopted when the learned decoder's FER is
+    nowhere worse than the plain decoder's at --plain-iters (load_weights
+    ignores files that are not)."""
     import argparse
     import time
     ap = argparse.ArgumentParser()
@@ -286,7 +301,8 @@ def main(argv=None):
     rows = fer_table(args.modcod, fs, grid, [("plain%d" % args.plain_iters, args.plain_iters, None),
                                               ("plain%d" % T, T, None), ("learned%d" % T, T, w)],
                      max_frames=args.fer_frames, log=print)
-    meta = {"train": {"frames": args.frames, "batch": args.batch, "lr": args.lr, "beta_lr_scale": args.beta_lr_scale,
+    ok = adopted(rows, "learned%d" % T, "plain%d" % args.plain_iters)
+    meta = {"adopted": ok, "train": {"frames": args.frames, "batch": args.batch, "lr": args.lr, "beta_lr_scale": args.beta_lr_scale,
                       "loss": args.loss, "esn0_grid_db": [round(g, 3) for g in grid], "seconds": round(train_s, 1),
                       "loss_history": [[int(a), float(b)] for a, b in hist], "seed": args.seed},
             "fer": rows, "fer_rule": "200 frame errors or %d frames per point" % args.fer_frames}

@@ -117,3 +117,24 @@ def test_training_lowers_loss_and_quantises(cuda):
     assert w.dtype == np.int16 and (w[..., 1] >= 1).all()
     res = learned.frame_errors(name, fs, thr + 0.5, T, w, n_frames=512, batch=128)
     assert res["frames"] == 512 and 0 <= res["fer"] <= 1
+
+
+def test_committed_weights_beat_plain(cuda):
+    """The adopted weights of normal QPSK 1/3 (trained on 1e6 frames by the
+    kernels above): 0.25 dB below the MODCOD's threshold the learned decoder
+    capped at 20 iterations decodes frames that the plain decoder capped at 50
+    loses, and at the threshold it needs fewer than half the iterations."""
+    name, fs = "qpsk1/3", NORMAL
+    w = learned.load_weights(name, fs)
+    assert w is not None and w.shape == (20, 32, 2)
+    thr = E.find_modcod(name)[5]
+    low_p = learned.frame_errors(name, fs, thr - 0.25, 50, None, n_frames=512, batch=256, seed=31)
+    low_l = learned.frame_errors(name, fs, thr - 0.25, 20, w, n_frames=512, batch=256, seed=31)
+    assert low_p["fer"] > 0.2 and low_l["frame_errors"] <= 2, (low_p, low_l)
+    at_p = learned.frame_errors(name, fs, thr, 50, None, n_frames=512, batch=256, seed=32)
+    at_l = learned.frame_errors(name, fs, thr, 20, w, n_frames=512, batch=256, seed=32)
+    assert at_l["frame_errors"] <= at_p["frame_errors"]
+    assert at_l["mean_iterations"] < 0.5 * at_p["mean_iterations"], (at_p, at_l)
+    # a weight file that lost to the plain decoder is not loaded
+    assert learned.load_weights("16apsk3/4", NORMAL) is None
+    assert learned.load_weights("16apsk3/4", NORMAL, adopted_only=False) is not None
