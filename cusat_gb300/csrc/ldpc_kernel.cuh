@@ -123,10 +123,18 @@ __device__ __forceinline__ void load_row(uint4 (&dst)[RW], const uint4* src, boo
         dst[w] = pred ? __ldcg(src + w) : make_uint4(0, 0, 0, 0);
 }
 
+// Integer adds of the check loop issue as multiply-adds: the kernel is bound
+// by the integer ALU pipe while the multiply-add pipe idles, and x * k + y
+// with k read from constant memory (value 1 or -1, unknown to the compiler)
+// becomes one IMAD on that pipe.  Same results as x + y.
+static __constant__ int c_pipe_one = 1;
+
+__device__ __forceinline__ int madd(int x, int k, int y) { return x * k + y; }
+
 // (j + r) mod 360 for j, r in [0, 360)
-__device__ __forceinline__ int rot360(int j, uint32_t r)
+__device__ __forceinline__ int rot360(int j, uint32_t r, int one)
 {
-    const unsigned u = (unsigned)j + r;
+    const unsigned u = (unsigned)madd((int)r, one, j);
     return (int)__viaddmin_u32(u, (unsigned)(-kM), u);
 }
 
@@ -166,7 +174,7 @@ __device__ bool syndrome_ok(const unsigned char* smem, const SmemCode& t, int K,
 #pragma unroll
                 for (int e = 0; e < CMAX; e++) {
                     const uint2 w = tb[e];
-                    x ^= lds16(smem, (int)w.x + 2 * rot360(j, w.y & 0x1ff));
+                    x ^= lds16(smem, (int)w.x + 2 * rot360(j, w.y & 0x1ff, 1));
                 }
                 bad |= x;
             }
@@ -210,24 +218,29 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
                                               uint4* dst, int trial)
 {
     constexpr int NE = CMAX + 2;
+    // Wide rows would not fit the register budget with every slot's store
+    // address held from the gather to the scatter: they recompute it there.
+    constexpr bool kKeepAddr = CMAX <= 14;
+    const int one = c_pipe_one, neg = -one, two = one + one;
     int d[NE];
-    int sa[CMAX];  // where each slot's update is stored (its APP slot, or stage/junk)
+    int sa[kKeepAddr ? CMAX : 1];  // where each slot's update is stored (its APP slot, or stage/junk)
     // gather: two parity edges (the second absent for check 0 of layer 0,
     // which then reads and writes a scratch slot), then the circulants
     const int a0 = lds16(smem, ps0);
     const int a1 = lds16(smem, ps1);
     {
-        const int x0 = a0 - row_byte(cur, 0);
-        const int x1 = a1 - row_byte(cur, 1);
+        const int x0 = madd(row_byte(cur, 0), neg, a0);
+        const int x1 = madd(row_byte(cur, 1), neg, a1);
         d[0] = SAT ? sat16(x0) : x0;
         d[1] = absent ? kBig : (SAT ? sat16(x1) : x1);
     }
 #pragma unroll
     for (int e = 0; e < CMAX; e++) {
         const uint2 w = tb[e];
-        const int ad = (int)w.x + 2 * rot360(j, w.y & 0x1ff);
-        sa[e] = ad + ((int)w.y >> 9);
-        const int x = lds16(smem, ad) - row_byte(cur, e + 2);
+        const int ad = madd(rot360(j, w.y & 0x1ff, one), two, (int)w.x);
+        if (kKeepAddr)
+            sa[e] = madd((int)w.y >> 9, one, ad);
+        const int x = madd(row_byte(cur, e + 2), neg, lds16(smem, ad));
         d[2 + e] = SAT ? sat16(x) : x;
     }
     // check node: min1/min2 of |extrinsic|, sign product
@@ -251,7 +264,7 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
     }
     // each message carries the sign product of the other edges
     const int sg = sx >> 31;
-    const int p1 = (m1 ^ sg) - sg, p2 = (m2 ^ sg) - sg;
+    const int p1 = madd(sg, neg, m1 ^ sg), p2 = madd(sg, neg, m2 ^ sg);
     uint32_t wv[RW * 4];
 #pragma unroll
     for (int k = 0; k < RW * 4; k++)
@@ -259,24 +272,31 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
 #pragma unroll
     for (int e = 0; e < NE; e++) {
         const int ds = d[e] >> 31;
-        const int mg = (((abs(d[e]) == r1) ? p2 : p1) ^ ds) - ds;
+        const int mg = madd(ds, neg, ((abs(d[e]) == r1) ? p2 : p1) ^ ds);
         wv[e >> 2] = __byte_perm(wv[e >> 2], (uint32_t)mg,
                                  (e & 3) == 0 ? 0x3214 : (e & 3) == 1 ? 0x3240 : (e & 3) == 2 ? 0x3410 : 0x4210);
         if (e < 2) {
             // parity: APP = sat16(extrinsic + message)
-            sts16(smem, e == 0 ? ps0 : ps1, SAT ? sat16(d[e] + mg) : d[e] + mg);
+            sts16(smem, e == 0 ? ps0 : ps1, SAT ? sat16(d[e] + mg) : madd(mg, one, d[e]));
         } else {
+            int at;
+            if (kKeepAddr) {
+                at = sa[e - 2];
+            } else {
+                const uint2 w = tb[e - 2];
+                at = madd((int)w.y >> 9, one, madd(rot360(j, w.y & 0x1ff, one), two, (int)w.x));
+            }
             int v;
             if (SAT) {
                 // re-read the APP (unchanged: no other check of the step
                 // writes this bit); a staged slot stores its delta, the
                 // completion saturates the sum once
                 const int delta = mg - row_byte(cur, e);
-                v = ((int)tb[e - 2].y >> 9) == 0 ? sat16(lds16(smem, sa[e - 2]) + delta) : delta;
+                v = ((int)tb[e - 2].y >> 9) == 0 ? sat16(lds16(smem, at) + delta) : delta;
             } else {
-                v = d[e] + mg;
+                v = madd(mg, one, d[e]);
             }
-            sts16(smem, sa[e - 2], v);
+            sts16(smem, at, v);
         }
     }
 #pragma unroll
