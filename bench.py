@@ -44,10 +44,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "LDPC decode info Gbit/s at equal FER (plain vs learned MS); p99 frame latency"
-WORKLOAD = {"name": "normal 3/5 8PSK", "fs": 0, "rate": 4, "mod": 1, "frames": 256, "esn0_db": 6.0,
-            "max_trials": 50, "seed": 2024}
-N_BUFS = 4
-PIPE = 2
+WORKLOAD = {"name": "normal 3/5 8PSK", "code": "s2_b5", "mod_name": "8PSK", "fs": 0, "rate": 4, "mod": 1,
+            "frames": 256, "esn0_db": 6.0, "max_trials": 50, "seed": 2024}
+# short FECFRAME 1/2 QPSK, 64 frames at 1.5 dB (the reference's CPU-runnable case)
+WORKLOAD_SHORT = {"name": "short 1/2 QPSK", "code": "s2_c4", "mod_name": "QPSK", "fs": 1, "rate": 3, "mod": 0,
+                  "frames": 64, "esn0_db": 1.5, "max_trials": 50, "seed": 2025}
+N_BUFS = 4          # input batches cycled through (at least; more when a batch is small)
+L2_BYTES = 160e6    # cycled inputs exceed this (GB300 L2: 129 MB)
+PIPE = 2            # chains (streams) whose consecutive batches overlap, at least
+RESIDENT_CTAS = 304 # resident decoder CTAs on a GB300 (152 SMs x 2 for short frames)
+
+
+def n_bufs_for(wl):
+    """Batches to cycle through so that the inputs exceed the L2."""
+    import cusat_gb300 as cs
+    mi = cs.modcod_info(wl["mod"], wl["rate"], wl["fs"])
+    batch_bytes = wl["frames"] * mi["xfecframe_len"] * 8
+    return max(N_BUFS, int(np.ceil(L2_BYTES / batch_bytes)))
 
 
 def parse():
@@ -57,8 +70,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames in the CPU sample (0 = auto)")
-    ap.add_argument("--workload", choices=["single", "mixed", "serve", "learned"], default="single",
-                    help="single: the headline 8PSK 3/5 batch; mixed: 1024 frames of 10 MODCODs in a CUDA graph; "
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall time of the CPU baseline sample")
+    ap.add_argument("--workload", choices=["single", "short", "mixed", "serve", "learned", "codes"],
+                    default="single",
+                    help="single: the headline 8PSK 3/5 batch; short: 64 short QPSK 1/2 frames; mixed: 1024 frames of 10 MODCODs in a CUDA graph; "
                          "serve: Poisson arrivals through the serving loop; learned: plain (max 50 it) vs "
                          "learned (max 20 it) min-sum on normal QPSK 1/3 at its threshold")
     ap.add_argument("--rates", default="0.5,1,2,3,4,5", help="serve: aggregate Gsym/s to sweep")
@@ -157,13 +172,25 @@ def cpu_chain(wl, bufs, n0, gain, n_frames, threads):
     return time.perf_counter() - t0, trials
 
 
+def cpu_sample(wl, bufs, n0, gain, threads, seconds):
+    """Oracle chain over the workload's batches (cycled) until `seconds` of
+    wall time have passed; returns (seconds, frames)."""
+    total, frames, k = 0.0, 0, 0
+    while total < seconds:
+        dt, _ = cpu_chain(wl, [bufs[k % len(bufs)]], n0, gain, wl["frames"], threads)
+        total += dt
+        frames += wl["frames"]
+        k += 1
+    return total, frames
+
+
 def reference_arm(args, wl):
     rank, _, world = dist_env()
     if rank != 0:
         return
     ci, msg, bufs, n0, gain = make_traffic(wl, 1)
     threads = os.cpu_count() or 1
-    n = args.cpu_sample or max(threads, 16)
+    n = args.cpu_sample or wl["frames"]
     for _ in range(args.warmup):
         cpu_chain(wl, bufs, n0, gain, min(n, 4), threads)
     total = 0.0
@@ -174,7 +201,7 @@ def reference_arm(args, wl):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
-            "data": "synthetic (seeded BCH/LDPC-encoded 8PSK frames, AWGN)",
+            "data": f"synthetic (seeded BCH/LDPC-encoded {wl['mod_name']} frames, AWGN)",
             "config": {"workload": f"{wl['name']}: CPU demap + layered min-sum decode (max "
                                    f"{wl['max_trials']} it) + BCH check, {n} frames per step",
                        "frames": n, "esn0_db": wl["esn0_db"], "max_trials": wl["max_trials"]},
@@ -194,7 +221,7 @@ def load_peaks():
 
 def main():
     args = parse()
-    wl = dict(WORKLOAD)
+    wl = dict(WORKLOAD_SHORT if args.workload == "short" else WORKLOAD)
     if args.impl == "reference":
         if args.workload == "mixed":
             mixed_reference_arm(args)
@@ -210,29 +237,33 @@ def main():
     import cusat_gb300 as cs
     from cusat_gb300 import build as lib_build
     lib_build.build()
-    if args.workload in ("mixed", "serve", "learned"):
-        {"mixed": mixed_main, "serve": serve_main, "learned": learned_main}[args.workload](
+    if args.workload in ("mixed", "serve", "learned", "codes"):
+        {"mixed": mixed_main, "serve": serve_main, "learned": learned_main, "codes": codes_main}[args.workload](
             args, torch, cs, rank, local_rank, world)
         if world > 1:
             torch.distributed.destroy_process_group()
         return
 
-    ci, msg, bufs, n0, gain = make_traffic(wl, N_BUFS)
+    nb = n_bufs_for(wl)
+    ci, msg, bufs, n0, gain = make_traffic(wl, nb)
     B, T = wl["frames"], wl["max_trials"]
     # two chains on two streams: consecutive batches overlap, so the SMs that
     # finish one batch's last frames start on the next batch
-    rxs = [cs.rx_fec(wl["mod"], wl["rate"], wl["fs"], T, B) for _ in range(PIPE)]
-    streams = [torch.cuda.Stream() for _ in range(PIPE)]
+    # enough chains in flight that small batches (64 short frames) fill the
+    # resident CTA slots
+    pipe = min(8, max(PIPE, -(-RESIDENT_CTAS // B)))
+    rxs = [cs.rx_fec(wl["mod"], wl["rate"], wl["fs"], T, B) for _ in range(pipe)]
+    streams = [torch.cuda.Stream() for _ in range(pipe)]
     d_sym = [torch.from_numpy(b).cuda() for b in bufs]
     h_sym = [torch.from_numpy(b).pin_memory() for b in bufs]
     k_bytes = rxs[0].k_bytes
     outs = [(torch.zeros((B, k_bytes), dtype=torch.uint8, device="cuda"),
              torch.zeros(B, dtype=torch.int32, device="cuda"),
-             torch.zeros(B, dtype=torch.int32, device="cuda")) for _ in range(PIPE)]
-    d_in = [torch.empty_like(d_sym[0]) for _ in range(PIPE)]
+             torch.zeros(B, dtype=torch.int32, device="cuda")) for _ in range(pipe)]
+    d_in = [torch.empty_like(d_sym[0]) for _ in range(pipe)]
     h_out = [(torch.empty((B, k_bytes), dtype=torch.uint8).pin_memory(),
               torch.empty(B, dtype=torch.int32).pin_memory(),
-              torch.empty(B, dtype=torch.int32).pin_memory()) for _ in range(PIPE)]
+              torch.empty(B, dtype=torch.int32).pin_memory()) for _ in range(pipe)]
 
     def barrier():
         torch.cuda.synchronize()
@@ -241,17 +272,17 @@ def main():
         torch.cuda.synchronize()
 
     def step(i, e2e):
-        k = i % PIPE
+        k = i % pipe
         st = streams[k]
         hard, trials, valid = outs[k]
         with torch.cuda.stream(st):
             if e2e:
-                d_in[k].copy_(h_sym[i % N_BUFS], non_blocking=True)
+                d_in[k].copy_(h_sym[i % nb], non_blocking=True)
                 rxs[k].launch(d_in[k], B, n0, gain, hard, trials, valid, st)
                 for h, d in zip(h_out[k], outs[k]):
                     h.copy_(d, non_blocking=True)
             else:
-                rxs[k].launch(d_sym[i % N_BUFS], B, n0, gain, hard, trials, valid, st)
+                rxs[k].launch(d_sym[i % nb], B, n0, gain, hard, trials, valid, st)
 
     def timed(e2e):
         for i in range(args.warmup):
@@ -316,38 +347,47 @@ def main():
     peaks = load_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     achieved = per_launch_bytes / launch_s / 1e9
+    traffic, prof = None, {}
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json"))).get(args.workload, {})
+        traffic = prof["dram_read_bytes"] + prof["dram_write_bytes"]
+    except (OSError, KeyError, ValueError):
+        pass
     edge_iters = float(np.mean(it)) * ci["edges"] * B
     threads = os.cpu_count() or 1
-    n_cpu = max(threads, 16)
-    cpu_s, _ = cpu_chain(wl, bufs, n0, gain, n_cpu, threads)
+    cpu_s, n_cpu = cpu_sample(wl, bufs, n0, gain, threads, args.cpu_seconds)
     cpu_value = n_cpu * ci["k_ldpc"] / cpu_s / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16",
-        "data": "synthetic (seeded BCH/LDPC-encoded 8PSK frames, AWGN at Es/N0 6.0 dB)",
-        "config": {"workload": "normal 3/5 8PSK (s2_b5), 256 frames, Es/N0 6.0 dB: fused demap + "
-                               "deinterleave -> layered min-sum LDPC (max 50 it) -> BCH check",
+        "data": f"synthetic (seeded BCH/LDPC-encoded {wl['mod_name']} frames, AWGN at Es/N0 {wl['esn0_db']} dB)",
+        "config": {"workload": f"{wl['name']} ({wl['code']}), {B} frames, Es/N0 {wl['esn0_db']} dB: fused demap + "
+                               f"deinterleave -> layered min-sum LDPC (max {T} it) -> BCH check",
                    "frames": B, "max_trials": T, "esn0_db": wl["esn0_db"], "decoder": "plain offset min-sum",
-                   "parallelism": f"replicas x{world}; {PIPE} chains on {PIPE} streams, consecutive batches "
+                   "parallelism": f"replicas x{world}; {pipe} chains on {pipe} streams, consecutive batches "
                                   f"overlap",
                    "launch_ms": launch_ms,
-                   "l2": f"inputs cycled over {N_BUFS} batches ({N_BUFS * bufs[0].nbytes / 1e6:.0f} MB > L2)",
+                   "l2": f"inputs cycled over {nb} batches ({nb * bufs[0].nbytes / 1e6:.0f} MB > L2)",
                    "mean_iterations": float(np.mean(it)), "p99_iterations": float(np.percentile(it, 99)),
                    "frames_failed": int(np.sum(it >= T))},
         "e2e": {"value": e2e, "unit": "Gbit/s", "h2d_bytes_per_step": int(bufs[0].nbytes),
                 "d2h_bytes_per_step": int(B * (k_bytes + 8))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": traffic, "algorithmic_bytes": per_launch_bytes,
                      "note": "algorithmic HBM bytes per launch (8 B/symbol in, k/8 + 12 B/frame out) over the "
-                             "fused chain's launch time; peak = measured copy bandwidth"},
+                             "fused chain's launch time (CUDA events), peak = measured copy bandwidth (of measured); "
+                             "traffic = DRAM bytes of one decoder launch from the ncu capture in "
+                             "profiles/ (null when none was taken for this workload); the decoder is bound "
+                             "by the integer ALU pipe (onchip)"},
         "onchip": {"edge_iterations_per_s": edge_iters / launch_s,
+                   "alu_pipe_pct_ncu": prof.get("alu_pipe_pct"), "issue_active_pct_ncu": prof.get("issue_active_pct"),
                    "smem_app_bytes_per_s": 4.0 * edge_iters / launch_s,
                    "note": "mean iterations x Tanner edges x frames per launch; 4 B of shared-memory APP "
                            "traffic per edge-iteration (gather + scatter), messages 2 B in L2"},
         "cpu_baseline": {"value": cpu_value, "unit": "Gbit/s", "cores": threads, "kind": "port",
-                         "sample": f"{n_cpu} frames of the workload through the C oracle (demap + decode + "
-                                   f"BCH), {cpu_s:.1f} s"},
+                         "sample": f"{n_cpu} frames of the workload ({n_cpu // B} batches) through the C oracle "
+                                   f"(demap + decode + BCH), {cpu_s:.1f} s on {threads} threads"},
         "clocks": clk,
         "gpu_launches": 2 * args.steps,
         "wall_s": wall,
@@ -554,8 +594,13 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
     hbm_peak = load_peaks().get("hbm_gbs", 6800.0)
     achieved = (in_bytes + out_bytes) / (lat_ms * 1e-3) / 1e9
     threads = os.cpu_count() or 1
-    n_cpu = args.cpu_sample or 128
-    cpu_s, cpu_bits = cpu_mixed(mt, n_cpu, threads, T)
+    n_cpu = args.cpu_sample or n
+    cpu_s, cpu_bits, reps = 0.0, 0, 0
+    while cpu_s < args.cpu_seconds:
+        dt, b = cpu_mixed(mt, n_cpu, threads, T)
+        cpu_s += dt
+        cpu_bits += b
+        reps += 1
     print(json.dumps({
         "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -579,7 +624,8 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
                      "note": "algorithmic bytes (symbols in, hard bits + counters out) per replay over the "
                              "replay time; the decoders are bound by the integer ALU pipe"},
         "cpu_baseline": {"value": cpu_bits / cpu_s / 1e9, "unit": "Gbit/s", "cores": threads, "kind": "port",
-                         "sample": f"first {n_cpu} frames through the C oracle, {cpu_s:.1f} s"},
+                         "sample": f"{reps} x the first {n_cpu} frames through the C oracle, {cpu_s:.1f} s on "
+                                   f"{threads} threads"},
         "clocks": clk,
         "gpu_launches": args.steps * (n_classes + 1),
     }), flush=True)
@@ -639,7 +685,8 @@ def learned_main(args, torch, cs, rank, local_rank, world):
     w = learned.load_weights(wl["modcod"], wl["fs"])
     if w is None:
         raise RuntimeError("no adopted weight file for " + wl["modcod"])
-    ci, msg, bufs, n0, gain = make_traffic(wl, N_BUFS)
+    nb = n_bufs_for(wl)
+    ci, msg, bufs, n0, gain = make_traffic(wl, nb)
     B = wl["frames"]
     sent = [torch.from_numpy(cs.encode_frames(wl["fs"], wl["rate"], msg)[:, :ci["k_ldpc"] // 8]).cuda()]
     d_sym = [torch.from_numpy(b).cuda() for b in bufs]
@@ -655,7 +702,7 @@ def learned_main(args, torch, cs, rank, local_rank, world):
         def step(i):
             k = i % PIPE
             with torch.cuda.stream(streams[k]):
-                rxs[k].launch(d_sym[i % N_BUFS], B, n0, gain, outs[k][0], outs[k][1], None, streams[k])
+                rxs[k].launch(d_sym[i % nb], B, n0, gain, outs[k][0], outs[k][1], None, streams[k])
 
         for i in range(args.warmup):
             step(i)
@@ -697,6 +744,54 @@ def learned_main(args, torch, cs, rank, local_rank, world):
                    "learned": res["learned20"], "plain": res["plain50"],
                    "speedup": res["learned20"]["gbit_s"] / res["plain50"]["gbit_s"]},
     }), flush=True)
+
+
+CODES = [("qpsk1/4", 0), ("qpsk1/2", 1), ("qpsk1/2", 0), ("8psk3/5", 1), ("8psk3/5", 0), ("16apsk3/4", 1),
+         ("qpsk3/4", 0), ("16apsk5/6", 1), ("8psk5/6", 0), ("8psk8/9", 1), ("8psk9/10", 0)]
+
+
+def codes_main(args, torch, cs, rank, local_rank, world):
+    """One MODCOD per kernel class (circulant slots per layer x lanes): 256
+    frames at threshold + 0.5 dB through the fused chain, median of `steps`
+    single launches (CUDA events) after `warmup`; value = the headline
+    class's Gbit/s, the others in config.codes."""
+    from cusat_gb300 import traffic
+    from cusat_gb300.enums import find_modcod
+    B, rows = 256, {}
+    st = torch.cuda.current_stream()
+    for name, fs in CODES:
+        _, mod, rate, _, _, thr = find_modcod(name)
+        _, sym, n0, gain = traffic.modcod_frames(name, fs, B, thr + 0.5, np.random.default_rng(5))
+        ci = cs.code_info(fs, rate)
+        rx = cs.rx_fec(mod, rate, fs, 50, B)
+        d = torch.from_numpy(sym).cuda()
+        h = torch.zeros((B, rx.k_bytes), dtype=torch.uint8, device="cuda")
+        t = torch.zeros(B, dtype=torch.int32, device="cuda")
+        for _ in range(args.warmup):
+            rx.launch(d, B, n0, gain, h, t, None, st)
+        ts = []
+        for _ in range(max(args.steps, 3)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            rx.launch(d, B, n0, gain, h, t, None, st)
+            b.record(st)
+            st.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms = float(np.median(ts))
+        tr = t.cpu().numpy()
+        it = float(np.mean(np.where(tr >= 0, 50 - tr, 50)))
+        rows[f"{name} {'short' if fs else 'normal'}"] = {
+            "slots": ci["cmax"], "lanes": ci["lanes"], "launch_ms": ms, "gbit_s": B * ci["k_ldpc"] / ms / 1e6,
+            "mean_iterations": it, "edge_iterations_per_ns": B * it * ci["edges"] / ms / 1e6}
+    if rank != 0:
+        return
+    head = rows["8psk3/5 normal"]
+    print(json.dumps({
+        "metric": METRIC, "value": head["gbit_s"], "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["launch_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded frames at threshold + 0.5 dB)",
+        "config": {"workload": "one MODCOD per decoder kernel class, 256 frames, single launches (inputs in "
+                               "L2 for the short codes)", "codes": rows}}), flush=True)
 
 
 if __name__ == "__main__":
