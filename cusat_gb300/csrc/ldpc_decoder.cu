@@ -44,7 +44,7 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     };
     take(&a->sm_dummy, 2 * kM * 2);  // +32767 region, then the junk region
     take(&a->sm_stage, kStageSets * kMaxStage * kM * 2);
-    take(&a->sm_tab, d.q * d.cmax * 8);
+    take(&a->sm_tab, d.q * d.cmax * 16);
     take(&a->sm_cnt, d.q);
     take(&a->sm_sched, d.n_steps * 4);
     take(&a->sm_conf, d.n_steps);

@@ -84,7 +84,7 @@ struct Job {
 
 // Shared-memory views of the code tables.
 struct SmemCode {
-    const uint2* tab;  // per slot: x = bit base, y = r | store offset << 9
+    const uint4* tab;  // per slot: x = byte base, y = 2 r, z = store offset
     const uint8_t* cnt;
     const int16_t* sched;
     const uint8_t* conf;
@@ -131,11 +131,11 @@ static __constant__ int c_pipe_one = 1;
 
 __device__ __forceinline__ int madd(int x, int k, int y) { return x * k + y; }
 
-// (j + r) mod 360 for j, r in [0, 360)
-__device__ __forceinline__ int rot360(int j, uint32_t r, int one)
+// 2 ((j + r) mod 360) from j2 = 2 j and r2 = 2 r, j, r in [0, 360)
+__device__ __forceinline__ int rot720(int j2, uint32_t r2, int one)
 {
-    const unsigned u = (unsigned)madd((int)r, one, j);
-    return (int)__viaddmin_u32(u, (unsigned)(-kM), u);
+    const unsigned u = (unsigned)madd((int)r2, one, j2);
+    return (int)__viaddmin_u32(u, (unsigned)(-2 * kM), u);
 }
 
 __device__ __forceinline__ int lds16(const unsigned char* smem, int off)
@@ -170,11 +170,11 @@ __device__ bool syndrome_ok(const unsigned char* smem, const SmemCode& t, int K,
                     x ^= lds16(smem, pty + 2 * ((i - 1) * kM + j));
                 else if (j > 0)
                     x ^= lds16(smem, pty + 2 * ((q - 1) * kM + j - 1));
-                const uint2* tb = t.tab + i * CMAX;
+                const uint4* tb = t.tab + i * CMAX;
 #pragma unroll
                 for (int e = 0; e < CMAX; e++) {
-                    const uint2 w = tb[e];
-                    x ^= lds16(smem, (int)w.x + 2 * rot360(j, w.y & 0x1ff, 1));
+                    const uint4 w = tb[e];
+                    x ^= lds16(smem, (int)w.x + rot720(2 * j, w.y, 1));
                 }
                 bad |= x;
             }
@@ -213,7 +213,7 @@ __device__ __forceinline__ int scaled_mag(int r, int beta, int alpha)
 // row; straight-line code for every layer (plain, staged and absent slots
 // differ only in their descriptors).
 template <int CMAX, int RW, bool SAT>
-__device__ __forceinline__ void process_check(const int16_t* wts, unsigned char* smem, const uint2* tb, int cnt,
+__device__ __forceinline__ void process_check(const int16_t* wts, unsigned char* smem, const uint4* tb, int cnt,
                                               int j, int ps0, int ps1, bool absent, const uint4 (&cur)[RW],
                                               uint4* dst, int trial)
 {
@@ -221,7 +221,8 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
     // Wide rows would not fit the register budget with every slot's store
     // address held from the gather to the scatter: they recompute it there.
     constexpr bool kKeepAddr = CMAX <= 14;
-    const int one = c_pipe_one, neg = -one, two = one + one;
+    const int one = c_pipe_one, neg = -one;
+    const int j2 = j + j;
     int d[NE];
     int sa[kKeepAddr ? CMAX : 1];  // where each slot's update is stored (its APP slot, or stage/junk)
     // gather: two parity edges (the second absent for check 0 of layer 0,
@@ -236,10 +237,10 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
     }
 #pragma unroll
     for (int e = 0; e < CMAX; e++) {
-        const uint2 w = tb[e];
-        const int ad = madd(rot360(j, w.y & 0x1ff, one), two, (int)w.x);
+        const uint4 w = tb[e];
+        const int ad = madd(rot720(j2, w.y, one), one, (int)w.x);
         if (kKeepAddr)
-            sa[e] = madd((int)w.y >> 9, one, ad);
+            sa[e] = madd((int)w.z, one, ad);
         const int x = madd(row_byte(cur, e + 2), neg, lds16(smem, ad));
         d[2 + e] = SAT ? sat16(x) : x;
     }
@@ -283,8 +284,8 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
             if (kKeepAddr) {
                 at = sa[e - 2];
             } else {
-                const uint2 w = tb[e - 2];
-                at = madd((int)w.y >> 9, one, madd(rot360(j, w.y & 0x1ff, one), two, (int)w.x));
+                const uint4 w = tb[e - 2];
+                at = madd((int)w.z, one, madd(rot720(j2, w.y, one), one, (int)w.x));
             }
             int v;
             if (SAT) {
@@ -292,7 +293,7 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
                 // writes this bit); a staged slot stores its delta, the
                 // completion saturates the sum once
                 const int delta = mg - row_byte(cur, e);
-                v = ((int)tb[e - 2].y >> 9) == 0 ? sat16(lds16(smem, at) + delta) : delta;
+                v = tb[e - 2].z == 0 ? sat16(lds16(smem, at) + delta) : delta;
             } else {
                 v = madd(mg, one, d[e]);
             }
@@ -341,18 +342,20 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
     int result = -1;
 
     for (int trial = 0;; trial++) {
+        // step 0's message rows are requested before the syndrome pass so
+        // that its latency hides behind it (unused when the frame converged)
+        const bool load = trial > 0 && trial < T;
+        uint4 cur[RW];
+        {
+            const int i0 = t.sched[lane];
+            load_row<RW>(cur, msg_cta + ((size_t)max(i0, 0) * kM + j) * RW, load && active && i0 >= 0);
+        }
         if (syndrome_ok<CMAX>(smem, t, K, q, n_steps, lane, j, active)) {
             result = T - trial;
             break;
         }
         if (trial == T)
             break;
-        const bool load = trial > 0;
-        uint4 cur[RW];
-        {
-            const int i0 = t.sched[lane];
-            load_row<RW>(cur, msg_cta + ((size_t)max(i0, 0) * kM + j) * RW, load && active && i0 >= 0);
-        }
         for (int s = 0; s < n_steps; s++) {
             const int i = t.sched[2 * s + lane];
             uint4 nxt[RW];
@@ -475,7 +478,7 @@ __device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCod
 {
     DevCode* s_code = reinterpret_cast<DevCode*>(smem + a.sm_code);
     DevDemap* s_dm = reinterpret_cast<DevDemap*>(smem + a.sm_code + sizeof(DevCode) + 8);
-    uint2* s_tab = reinterpret_cast<uint2*>(smem + a.sm_tab);
+    uint4* s_tab = reinterpret_cast<uint4*>(smem + a.sm_tab);
     uint8_t* s_cnt = smem + a.sm_cnt;
     int16_t* s_sched = reinterpret_cast<int16_t*>(smem + a.sm_sched);
     uint8_t* s_conf = smem + a.sm_conf;
@@ -492,7 +495,7 @@ __device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCod
             w.z += (uint32_t)a.sm_stage;
         else if (w.w == kSlotAbsent)
             w.x = (uint32_t)a.sm_dummy;
-        s_tab[k] = make_uint2(w.x, w.y | (w.z << 9));
+        s_tab[k] = make_uint4(w.x, 2 * w.y, w.z, 0);
     }
     for (int k = threadIdx.x; k < gc.q; k += blockDim.x) {
         int n = 0;
@@ -524,7 +527,7 @@ __global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc
     const DevDemap& dm = *reinterpret_cast<const DevDemap*>(smem + a.sm_code + sizeof(DevCode) + 8);
     const float2* pts = reinterpret_cast<const float2*>(smem + a.sm_pts);
     int* s_misc = reinterpret_cast<int*>(smem + a.sm_misc);
-    const SmemCode t = {reinterpret_cast<const uint2*>(smem + a.sm_tab), smem + a.sm_cnt,
+    const SmemCode t = {reinterpret_cast<const uint4*>(smem + a.sm_tab), smem + a.sm_cnt,
                         reinterpret_cast<const int16_t*>(smem + a.sm_sched), smem + a.sm_conf,
                         reinterpret_cast<const uint16_t*>(smem + a.sm_item_off),
                         reinterpret_cast<const uint2*>(smem + a.sm_items)};
