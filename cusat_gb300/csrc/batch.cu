@@ -243,7 +243,7 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
     // message scratch for every resident CTA, stream
     for (size_t k = 0; k < b->classes.size() && rc == CUSAT_OK; k++) {
         KernelClass& c = b->classes[k];
-        cusat::SmemDims dims{0, 0, 0, 0, c.cmax, 0};
+        cusat::SmemDims dims{0, 0, 0, 0, c.cmax, 0, c.lanes};
         size_t msg_cta = 0;
         std::vector<cusat::DevCode> codes;
         std::vector<cusat::DevDemap> demaps;

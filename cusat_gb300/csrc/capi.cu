@@ -67,7 +67,7 @@ struct Engine {
         memset(&proto, 0, sizeof(proto));
         proto.code = dp.code;
         proto.max_trials = max_trials;
-        cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, n_points));
+        cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, n_points, p->lanes));
         int optin = 0, sms = 0;
         CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");

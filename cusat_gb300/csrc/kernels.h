@@ -36,14 +36,14 @@ struct DecoderKernelInfo {
 
 // Largest code dimensions a decoder launch must hold in shared memory.
 struct SmemDims {
-    int N, q, n_steps, n_items, cmax, n_points;
+    int N, q, n_steps, n_items, cmax, n_points, lanes;
 };
 
 // The kernel instantiation for (cmax, lanes, fused), or nullptr.
 const void* select_decoder_kernel(int cmax, int lanes, bool fused);
 // Fills the shared-memory carve-up of a for codes up to d.
 void decoder_smem_layout(DecodeArgs* a, const SmemDims& d);
-SmemDims smem_dims_of(const DevCode& c, int n_points);
+SmemDims smem_dims_of(const DevCode& c, int n_points, int lanes);
 int decoder_threads(int lanes);
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
 

@@ -53,12 +53,15 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     take(&a->sm_pts, d.n_points * 8);
     take(&a->sm_code, (int)(sizeof(DevCode) + 8 + sizeof(DevDemap)));
     take(&a->sm_misc, 16);
+    // message rows staged for the next step: two sets x threads x row words
+    const int rw = (d.cmax + 2 + 15) / 16;
+    take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * kLaneThreads * rw * 16 : 0);
     a->sm_total = off;
 }
 
-SmemDims smem_dims_of(const DevCode& c, int n_points)
+SmemDims smem_dims_of(const DevCode& c, int n_points, int lanes)
 {
-    return SmemDims{c.N, c.q, c.n_steps, c.n_items, c.cmax, n_points};
+    return SmemDims{c.N, c.q, c.n_steps, c.n_items, c.cmax, n_points, lanes};
 }
 
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream)

@@ -70,7 +70,7 @@ struct DecodeArgs {
     int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
     unsigned int* queue;     // frame counter, zero at launch
     // shared-memory carve-up (bytes)
-    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_code, sm_misc,
+    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_code, sm_misc, sm_msgbuf,
         sm_total;
 };
 
@@ -122,6 +122,27 @@ __device__ __forceinline__ void load_row(uint4 (&dst)[RW], const uint4* src, boo
     for (int w = 0; w < RW; w++)
         dst[w] = pred ? __ldcg(src + w) : make_uint4(0, 0, 0, 0);
 }
+
+// Message rows of the next step are staged in shared memory by per-thread
+// asynchronous copies (cp.async, 16 bytes each, bypassing L1): a thread
+// copies and later reads only its own row, so it waits for its own copies
+// and no barrier is involved.  One commit group per step, empty when the
+// thread has nothing to copy.
+template <int RW>
+__device__ __forceinline__ void stage_row_async(uint4* dst, const uint4* src, bool pred)
+{
+    if (pred) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+#pragma unroll
+        for (int w = 0; w < RW; w++)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16 * w), "l"(src + w) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// all of this thread's copies but the most recent group have landed
+__device__ __forceinline__ void wait_staged_but_last() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void wait_staged_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Integer adds of the check loop issue as multiply-adds: the kernel is bound
 // by the integer ALU pipe while the multiply-add pipe idles, and x * k + y
@@ -339,16 +360,24 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
     const int pty = 2 * K;         // byte offset of the parity APP
     const int spare = 2 * c.N;     // scratch slot for the absent parity edge
     uint4* msg_cta = a.msg + (size_t)blockIdx.x * (size_t)a.msg_stride;
+    constexpr bool kSmemRows = stage_rows_in_smem(CMAX, LANES);
+    // staged rows (kSmemRows): set s & 1 holds this thread's row of step s
+    uint4* mrow = reinterpret_cast<uint4*>(smem + a.sm_msgbuf) + (size_t)tid * RW;
+    const int mset = (int)blockDim.x * RW;
     int result = -1;
 
     for (int trial = 0;; trial++) {
-        // step 0's message rows are requested before the syndrome pass so
-        // that its latency hides behind it (unused when the frame converged)
+        // step 0's rows are requested before the syndrome pass so that their
+        // latency hides behind it (left unread when the frame converged)
         const bool load = trial > 0 && trial < T;
         uint4 cur[RW];
         {
             const int i0 = t.sched[lane];
-            load_row<RW>(cur, msg_cta + ((size_t)max(i0, 0) * kM + j) * RW, load && active && i0 >= 0);
+            const uint4* src = msg_cta + ((size_t)max(i0, 0) * kM + j) * RW;
+            if (kSmemRows)
+                stage_row_async<RW>(mrow, src, load && active && i0 >= 0);
+            else
+                load_row<RW>(cur, src, load && active && i0 >= 0);
         }
         if (syndrome_ok<CMAX>(smem, t, K, q, n_steps, lane, j, active)) {
             result = T - trial;
@@ -361,7 +390,17 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
             uint4 nxt[RW];
             {
                 const int i_n = s + 1 < n_steps ? t.sched[2 * (s + 1) + lane] : -1;
-                load_row<RW>(nxt, msg_cta + ((size_t)max(i_n, 0) * kM + j) * RW, load && active && i_n >= 0);
+                const uint4* src = msg_cta + ((size_t)max(i_n, 0) * kM + j) * RW;
+                if (kSmemRows)
+                    stage_row_async<RW>(mrow + ((s + 1) & 1) * mset, src, load && active && i_n >= 0);
+                else
+                    load_row<RW>(nxt, src, load && active && i_n >= 0);
+            }
+            if (kSmemRows) {
+                wait_staged_but_last();
+#pragma unroll
+                for (int w = 0; w < RW; w++)
+                    cur[w] = (load && active && i >= 0) ? mrow[(s & 1) * mset + w] : make_uint4(0, 0, 0, 0);
             }
             if (active) {
                 // groups of the previous step whose completion was deferred
@@ -381,11 +420,15 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
                     complete_groups<LANES, SAT>(smem, stage, t, s, lane, j);
             }
             __syncthreads();
+            if (!kSmemRows) {
 #pragma unroll
-            for (int w = 0; w < RW; w++)
-                cur[w] = nxt[w];
+                for (int w = 0; w < RW; w++)
+                    cur[w] = nxt[w];
+            }
         }
     }
+    if (kSmemRows)
+        wait_staged_all();
     pack_hard(reinterpret_cast<const int16_t*>(smem), K, job.hard);
     if (threadIdx.x == 0)
         *job.trials = result;

@@ -176,7 +176,7 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     a.msg = (uint4*)st.msg;
     a.msg_stride = p->R * p->msg_row / 16;
     a.queue = st.queue;
-    cusat::decoder_smem_layout(&a, cusat::smem_dims_of(a.code, 0));
+    cusat::decoder_smem_layout(&a, cusat::smem_dims_of(a.code, 0, p->lanes));
     if (a.sm_total > st.optin)
         return fail(CUSAT_ERR_UNSUPPORTED, "frame state does not fit in shared memory");
     const void* fn = cusat::select_decoder_kernel(p->cmax, p->lanes, false);
