@@ -78,6 +78,8 @@ def parse():
                          "learned (max 20 it) min-sum on normal QPSK 1/3 at its threshold")
     ap.add_argument("--rates", default="0.5,1,2,3,4,5", help="serve: aggregate Gsym/s to sweep")
     ap.add_argument("--duration", type=float, default=0.25, help="serve: seconds of traffic per rate")
+    ap.add_argument("--learned", action="store_true",
+                    help="serve: decode each MODCOD with its adopted learned weights where one exists")
     return ap.parse_args()
 
 
@@ -638,7 +640,21 @@ def serve_main(args, torch, cs, rank, local_rank, world):
     info Gbit/s.  One line; value = info Gbit/s at the highest rate."""
     from cusat_gb300 import serving, traffic
     pool = serving.TracePool(traffic.MIXED_MODCODS, seed=2026 + rank, per_entry=16, torch=torch)
-    srv = cs.server(pool.modcods, max_trials=50, hbm_budget=4 << 30, slots=4, max_batch=512)
+    learned_entries = {}
+    if args.learned:
+        from cusat_gb300 import learned
+        for e, (name, fs) in enumerate(pool.table):
+            w = learned.load_weights(name, fs)
+            if w is not None:
+                learned_entries[e] = w
+
+    def new_server():
+        srv = cs.server(pool.modcods, max_trials=50, hbm_budget=4 << 30, slots=4, max_batch=512)
+        for e, w in learned_entries.items():
+            srv.set_weights(e, w)
+        return srv
+
+    srv = new_server()
     serving.replay(srv, pool, serving.make_trace(pool, 1e9, 0.02, seed=1))  # warm-up
     clocks = Clocks(local_rank)
     clocks.start()
@@ -651,7 +667,7 @@ def serve_main(args, torch, cs, rank, local_rank, world):
                     "peak_arena_mb": st["peak_bytes"] / 1e6})
         rows.append(row)
         srv.close()
-        srv = cs.server(pool.modcods, max_trials=50, hbm_budget=4 << 30, slots=4, max_batch=512)
+        srv = new_server()
     clk = clocks.stop()
     srv.close()
     if rank != 0:
@@ -664,6 +680,8 @@ def serve_main(args, torch, cs, rank, local_rank, world):
         "data": "synthetic (seeded ACM trace over 10 MODCODs, device-resident noisy frames at threshold + 0.5 dB)",
         "config": {"workload": "serving loop: Poisson arrivals, HBM-budget admission (4 GiB), continuous "
                                "batching on 4 slots (max 512 frames per batch), max 50 iterations",
+                   "learned_weights": sorted(f"{pool.table[e][0]} {'short' if pool.table[e][1] else 'normal'}"
+                                             for e in learned_entries),
                    "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "rates": rows},
         "clocks": clk,
     }), flush=True)

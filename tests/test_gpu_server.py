@@ -122,3 +122,26 @@ def test_learned_weights_per_modcod(cuda, pool):
         assert (r.trials, r.bch_valid) == (tr, vr) and (h == hr).all()
     assert any(e == learned_entry for e, _ in ref)
     srv.close()
+
+
+def test_host_symbols(cuda, pool):
+    """Requests whose symbols are in host memory (CUSAT_REQ_HOST_SYMBOLS) are
+    copied in at admission and decode like device-resident ones."""
+    torch = cuda
+    T = 25
+    srv = cs.server(pool.modcods, max_trials=T, hbm_budget=64 << 20, slots=2, max_batch=16)
+    picks = [(e, f) for e in range(len(pool.modcods)) for f in range(2)]
+    host = [np.ascontiguousarray(pool.entries[e]["sym"][f].cpu().numpy()) for e, f in picks]
+    hard = [np.zeros(pool.entries[e]["k_ldpc"] // 8, np.uint8) for e, _ in picks]
+    reqs = srv.requests([e for e, _ in picks], [pool.entries[e]["n0"] for e, _ in picks],
+                        [pool.entries[e]["gain"] for e, _ in picks], [h.ctypes.data for h in host],
+                        list(range(len(picks))), hard_host=[h.ctypes.data for h in hard], flags=cs.server.HOST_SYMBOLS)
+    srv.submit(reqs)
+    got = []
+    while len(got) < len(picks):
+        got += srv.poll(wait_ms=50)
+    got.sort(key=lambda r: r.tag)
+    for r, (e, f), h in zip(got, picks, hard):
+        hr, tr, vr = alone(torch, pool, e, f, T)
+        assert (r.trials, r.bch_valid) == (tr, vr) and (h == hr).all()
+    srv.close()
