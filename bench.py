@@ -79,7 +79,7 @@ def parse():
     ap.add_argument("--rates", default="0.5,1,2,3,4,5", help="serve: aggregate Gsym/s to sweep")
     ap.add_argument("--duration", type=float, default=0.25, help="serve: seconds of traffic per rate")
     ap.add_argument("--learned", action="store_true",
-                    help="serve: decode each MODCOD with its adopted learned weights where one exists")
+                    help="mixed/serve: decode each MODCOD with its adopted learned weights where one exists")
     return ap.parse_args()
 
 
@@ -507,6 +507,12 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
         h_hard = torch.empty(mt.hard_bytes, dtype=torch.uint8).pin_memory()
         h_res = torch.empty((2, n), dtype=torch.int32).pin_memory()
         b = cs.batch(mt.modcods, max_trials=T, max_frames=n)
+        if args.learned:
+            from cusat_gb300 import learned
+            for e, (name, _, _, fs) in enumerate(mt.table):
+                w = learned.load_weights(name, fs)
+                if w is not None:
+                    b.set_weights(e, w)
         fr = mt.descriptors(cs, d_sym, d_hard, d_res[0], d_res[1])
         torch.cuda.synchronize()
         tune_ms = b.tune(fr, reps=3, stream=streams[k])
@@ -612,7 +618,7 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
         "config": {"workload": "mixed: 1024 frames of 10 MODCODs (64APSK 32/45 for S2X 64APSK 2/3), 70% normal "
                                "/ 30% short, fused demap -> decode (max 50 it) -> BCH, one CUDA graph replay "
                                "per step (tuned grid and class order)",
-                   "frames": n, "max_trials": T, "kernel_classes": n_classes,
+                   "frames": n, "max_trials": T, "kernel_classes": n_classes, "learned_weights": bool(args.learned),
                    "parallelism": f"replicas x{world}; {S} graphs on {S} streams, consecutive batches overlap",
                    "l2": f"inputs alternate over {S} sets ({S * mt.sym.nbytes / 1e6:.0f} MB > L2)",
                    "batch_latency_ms": {"p50": lat_ms, "p99": float(np.percentile(lat, 99))},

@@ -31,8 +31,25 @@ def test_weight_files():
     for r in rows:
         for k in ("plain50", "plain20", "learned20"):
             assert r[k]["frame_errors"] >= 200 or r[k]["frames"] >= 1000000
-    assert learned.load_weights("16apsk3/4", E.FECFRAME_NORMAL) is None
-    assert learned.load_weights("qpsk1/2", E.FECFRAME_SHORT) is None
+    assert learned.load_weights("16apsk3/4", E.FECFRAME_NORMAL) is None    # not adopted
+    assert learned.load_weights("32apsk3/4", E.FECFRAME_NORMAL) is None    # no file
+
+
+def test_every_weight_file_is_consistent():
+    """Each stored table: right shape and ranges, its FER table present, and
+    its adoption flag what the adoption rule says."""
+    import glob
+    import os
+    files = glob.glob(os.path.join(learned.WEIGHTS_DIR, "*.json"))
+    assert len(files) >= 2
+    for f in files:
+        doc = json.load(open(f))
+        w = np.asarray(doc["weights"])
+        assert w.shape == (doc["n_iter"], 32, 2)
+        assert (w[..., 0] >= 0).all() and (w[..., 0] <= 127).all() and (w[..., 1] <= 255).all()
+        assert learned.weights_path(doc["modcod"], doc["framesize"]) == f
+        rows = doc["meta"]["fer"]
+        assert doc["meta"]["adopted"] == learned.adopted(rows, "learned%d" % doc["n_iter"], "plain50")
 
 
 def test_adoption_rule():
