@@ -424,7 +424,6 @@ class server:
                                                     slots, max_batch, ctypes.byref(h)))
         self._h = h
         self.modcods = [tuple(int(v) for v in r) for r in arr]
-        self._keep = []
 
     def close(self):
         if getattr(self, "_h", None):
@@ -452,7 +451,8 @@ class server:
         return arr
 
     def submit(self, reqs):
-        self._keep.append(reqs)
+        """Queues the requests (copied by the library; the symbols and host
+        hard-bit buffers they point to must stay valid until their results)."""
         _capi.check(_capi.lib().cusat_server_submit(self._h, ctypes.addressof(reqs), len(reqs)))
 
     def poll(self, max_results=4096, wait_ms=10):

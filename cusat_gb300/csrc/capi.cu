@@ -466,6 +466,10 @@ int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials,
     if (!out || max_trials < 0 || max_trials > 1000 || max_batch <= 0)
         return fail(CUSAT_ERR_ARG, "invalid arguments");
     *out = nullptr;
+    int dev;
+    int rc0 = require_device(&dev);
+    if (rc0)
+        return rc0;
     std::string err;
     const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
     if (!p)

@@ -36,6 +36,18 @@ def test_no_device_is_a_loud_error(built_lib):
     with pytest.raises(cs.CusatError) as e:
         cs.ldpc_decode_cuda(E.FECFRAME_SHORT, E.RATE_1_2, 50, 4)
     assert e.value.code == -4
+    # every object that needs the GPU refuses the same way
+    from cusat_gb300 import learned
+    makers = [lambda: cs.rx_fec(E.MOD_QPSK, E.RATE_1_2, E.FECFRAME_SHORT, 20, 4),
+              lambda: cs.demapper_cuda(E.MOD_8PSK, E.RATE_3_5, E.FECFRAME_NORMAL, 4),
+              lambda: cs.bch_check_cuda.for_code(E.FECFRAME_NORMAL, E.RATE_3_5),
+              lambda: cs.batch([(E.MOD_QPSK, E.RATE_1_2, E.FECFRAME_SHORT)], 20, 8),
+              lambda: cs.server([(E.MOD_QPSK, E.RATE_1_2, E.FECFRAME_SHORT)], 20, 64 << 20, 1, 8),
+              lambda: learned.nms_trainer(E.FECFRAME_SHORT, E.RATE_1_2, 5, 4)]
+    for make in makers:
+        with pytest.raises(cs.CusatError) as e:
+            make()
+        assert e.value.code == -4
 
 
 def test_invalid_arguments(built_lib):
