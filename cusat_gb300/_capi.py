@@ -70,6 +70,7 @@ _SIGS = {
                                                  ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_nms_trainer_destroy": (None, [ctypes.c_void_p]),
     "cusat_nms_trainer_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_nms_trainer_degree_counts": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
     "cusat_nms_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p]),

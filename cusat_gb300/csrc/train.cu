@@ -335,6 +335,7 @@ __global__ void __launch_bounds__(2 * kTrainLane, 1) nms_train_kernel(TrainArgs 
 struct cusat_nms_trainer {
     const cusat::CodePlan* plan = nullptr;
     int T = 0, max_batch = 0, grid = 0, deg_lo = 0, deg_hi = 0;
+    int deg_count[32] = {0};  // checks of each degree
     TrainArgs proto{};
     void* blob = nullptr;  // code tables
     float* bufs = nullptr; // L, gL, G
@@ -390,7 +391,9 @@ int cusat_nms_trainer_create(int framesize, int rate, int n_iter, int max_batch,
     for (int i = 0; i < q; i++) {
         t->deg_lo = std::min(t->deg_lo, (int)p->cnt[i] + (i == 0 ? 1 : 2));
         t->deg_hi = std::max(t->deg_hi, (int)p->cnt[i] + 2);
+        t->deg_count[p->cnt[i] + 2] += i == 0 ? kM - 1 : kM;
     }
+    t->deg_count[p->cnt[0] + 1] += 1;  // check 0 of layer 0 has no wrap edge
     const size_t o_sched = 0, n_sched = p->sched.size() * 2;
     const size_t o_cnt = (o_sched + n_sched + 255) / 256 * 256, n_cnt = p->cnt.size();
     const size_t o_ent = (o_cnt + n_cnt + 255) / 256 * 256, n_ent = ent.size() * 4;
@@ -450,6 +453,15 @@ int cusat_nms_trainer_info(const cusat_nms_trainer* t, int32_t* out)
     out[3] = t->max_batch;
     out[4] = t->deg_lo;
     out[5] = t->deg_hi;
+    return CUSAT_OK;
+}
+
+int cusat_nms_trainer_degree_counts(const cusat_nms_trainer* t, int32_t* counts)
+{
+    if (!t || !counts)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    for (int d = 0; d < 32; d++)
+        counts[d] = t->deg_count[d];
     return CUSAT_OK;
 }
 

@@ -35,6 +35,22 @@ class nms_trainer:
         out = (ctypes.c_int32 * 6)()
         _capi.check(_capi.lib().cusat_nms_trainer_info(h, out))
         self.n_ldpc, self.k_ldpc, self.n_iter, self.max_batch, self.deg_lo, self.deg_hi = list(out)
+        cnt = (ctypes.c_int32 * 32)()
+        _capi.check(_capi.lib().cusat_nms_trainer_degree_counts(h, cnt))
+        self.degree_counts = list(cnt)
+
+    def tied_degrees(self):
+        """{rare degree: degree it follows}: a degree with fewer checks than
+        one layer (check 0 of layer 0, which lacks the wrap edge) gets a
+        gradient from a handful of checks per frame; training ties it to the
+        next degree up instead of letting that noise steer it."""
+        out = {}
+        for d, n in enumerate(self.degree_counts):
+            if 0 < n < 360:
+                up = next((e for e in range(d + 1, 32) if self.degree_counts[e] >= 360), None)
+                if up is not None:
+                    out[d] = up
+        return out
 
     def close(self):
         if getattr(self, "_h", None):
@@ -182,8 +198,8 @@ def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128
     m = torch.zeros_like(theta)
     v = torch.zeros_like(theta)
     b1, b2, eps = 0.9, 0.999, 1e-8
-    used = torch.zeros((32,), dtype=torch.bool)
-    used[tr.deg_lo:tr.deg_hi + 1] = True
+    ties = tr.tied_degrees()
+    used = torch.tensor([n > 0 and d not in ties for d, n in enumerate(tr.degree_counts)])
     mask = used.cuda().view(1, 32, 1).expand_as(theta).float()
     history, acc, acc_n = [], 0.0, 0
     steps = max(1, n_frames // batch)
@@ -202,6 +218,8 @@ def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128
         theta.sub_(lr_k * scale * mh / (vh.sqrt() + eps))
         theta[:, :, 0].clamp_(0.0, 127.0)
         theta[:, :, 1].clamp_(1.0 / 64.0, 2.0)
+        for d, up in ties.items():
+            theta[:, d, :] = theta[:, up, :]
         acc += float(loss.item()) / batch
         acc_n += 1
         if log_every and (k + 1) % log_every == 0:

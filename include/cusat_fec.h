@@ -303,6 +303,8 @@ int cusat_nms_trainer_create(int framesize, int rate, int n_iter, int max_batch,
 void cusat_nms_trainer_destroy(cusat_nms_trainer* tr);
 /* out[0..5] = n_ldpc, k_ldpc, n_iter, max_batch, smallest and largest check degree */
 int cusat_nms_trainer_info(const cusat_nms_trainer* tr, int32_t* out);
+/* counts[d], d < 32: number of checks of degree d in the code */
+int cusat_nms_trainer_degree_counts(const cusat_nms_trainer* tr, int32_t* counts);
 /* batch frames of int16 LLRs (device, n_ldpc each, as the decoder takes them)
  * and their transmitted codewords (device, n_ldpc/8 bytes, MSB first);
  * theta_dev [n_iter][32][2] = {beta, alpha} (float, device); iter_w_dev

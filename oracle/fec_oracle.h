@@ -1,9 +1,9 @@
 /*
  * CPU oracle for the receive-side FEC path -- TEST INFRASTRUCTURE ONLY.
  *
- * A plain-C restatement of the reference's algorithms, used as the checker by
- * tests/, by __graft_entry__.smoke() and as the timed CPU baseline of
- * bench.py.  Nothing in the product (cusat_gb300/) links, loads or calls it.
+ * A plain-C restatement of the reference's algorithms that tests/ and
+ * __graft_entry__.smoke() compare the CUDA kernels against, and that bench.py
+ * times as the CPU baseline.  Nothing in the product (cusat_gb300/) links, loads or calls it.
  *
  * Decoder semantics (reference lib/cusat_dsp/cuda/ldpc_decode_kernel.cu):
  *   - APP init with the -32768 -> -32767 clamp and the parity transpose

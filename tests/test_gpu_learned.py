@@ -138,3 +138,15 @@ def test_committed_weights_beat_plain(cuda):
     # a weight file that lost to the plain decoder is not loaded
     assert learned.load_weights("16apsk3/4", NORMAL) is None
     assert learned.load_weights("16apsk3/4", NORMAL, adopted_only=False) is not None
+
+
+def test_degree_counts_and_ties(cuda):
+    tr = learned.nms_trainer(NORMAL, E.RATE_3_5, 3, 2)
+    ci = cs.code_info(NORMAL, E.RATE_3_5)
+    assert sum(tr.degree_counts) == ci["n_ldpc"] - ci["k_ldpc"]
+    assert tr.degree_counts[11] == ci["n_ldpc"] - ci["k_ldpc"] - 1 and tr.degree_counts[10] == 1
+    assert tr.tied_degrees() == {10: 11}
+    short = learned.nms_trainer(SHORT, E.RATE_1_2, 3, 2)
+    assert sum(short.degree_counts) == 16200 - 7200
+    for d, up in short.tied_degrees().items():
+        assert short.degree_counts[d] < 360 <= short.degree_counts[up]
