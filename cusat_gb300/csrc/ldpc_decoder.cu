@@ -33,7 +33,7 @@ const void* select_decoder_kernel(int cmax, int lanes, bool fused)
     }
 }
 
-int decoder_threads(int lanes) { return lanes * kLaneThreads; }
+int decoder_threads(int lanes) { return lanes * lane_threads(lanes); }
 
 void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
 {
@@ -55,7 +55,7 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     take(&a->sm_misc, 16);
     // message rows staged for the next step: two sets x threads x row words
     const int rw = (d.cmax + 2 + 15) / 16;
-    take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * kLaneThreads * rw * 16 : 0);
+    take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * lane_threads(d.lanes) * rw * 16 : 0);
     a->sm_total = off;
 }
 

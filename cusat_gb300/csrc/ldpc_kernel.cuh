@@ -1,8 +1,9 @@
 // Layered offset min-sum LDPC decoder for sm_103a.
 //
 // One CTA decodes one frame at a time and pulls frames from a queue
-// (persistent).  Each lane of 384 threads (12 warps) processes one layer of
-// the schedule step, thread j owning check row j (j < 360) of that layer;
+// (persistent).  Each lane processes one layer of the schedule step, thread
+// j owning check row j (j < 360) of that layer (with two lanes, 360 threads
+// each, lane 1 starts mid-warp);
 // LANES = 2 runs the paired layers of the reference's schedule side by side
 // (reference lib/cusat_dsp/cuda/ldpc_decode_kernel.cu:947-963).
 //
@@ -209,7 +210,10 @@ __device__ bool syndrome_ok(const unsigned char* smem, const SmemCode& t, int K,
 // Packs APP[0..K) < 0 MSB-first into K/8 bytes.
 __device__ __forceinline__ void pack_hard(const int16_t* app, int K, uint8_t* out)
 {
+    // full warps only (the block may end in a partial warp)
     const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (warp >= nw)
+        return;
     for (int base = warp * 32; base < K; base += nw * 32) {
         const int v = base + l;
         const bool neg = v < K && app[v] < 0;
@@ -353,8 +357,9 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
     constexpr int NE = CMAX + 2;
     constexpr int RW = (NE + 15) / 16;
     const int tid = threadIdx.x;
-    const int lane = (LANES == 2 && tid >= kLaneThreads) ? 1 : 0;
-    const int j = tid - lane * kLaneThreads;
+    constexpr int LT = lane_threads(LANES);
+    const int lane = (LANES == 2 && tid >= LT) ? 1 : 0;
+    const int j = tid - lane * LT;
     const bool active = j < kM;
     const int K = c.K, q = c.q, T = a.max_trials, n_steps = c.n_steps;
     const int pty = 2 * K;         // byte offset of the parity APP
@@ -560,7 +565,7 @@ __device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCod
 }
 
 template <int CMAX, int LANES, bool FUSED>
-__global__ void __launch_bounds__(LANES * kLaneThreads, LANES == 2 ? 1 : 2) ldpc_layered_kernel(DecodeArgs a)
+__global__ void __launch_bounds__(LANES * lane_threads(LANES), LANES == 2 ? 1 : 2) ldpc_layered_kernel(DecodeArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     int16_t* app = reinterpret_cast<int16_t*>(smem);
