@@ -28,6 +28,7 @@ from .enums import *  # noqa: F401,F403
 from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
 
 __all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch", "server",
+           "generator",
            "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
            "CusatError", "library_path"]
 
@@ -470,3 +471,26 @@ class server:
         keys = ["pending", "batches", "frames", "largest_batch", "max_inflight_batches", "peak_bytes",
                 "budget_bytes", "inflight_batches"]
         return dict(zip(keys, list(out)))
+
+
+class generator:
+    """Transmitter on the GPU: BCH + LDPC encode and map a batch of messages
+    (device memory in and out); equal bit for bit to encode_frames and
+    map_frames."""
+
+    def __init__(self, constellation, rate, framesize, max_batch=256):
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_generator_create(constellation, rate, framesize, max_batch, ctypes.byref(h)))
+        self._h = h
+        self.msg_bytes, self.cw_bytes, self.xfec, self.max_batch = _info(_capi.lib().cusat_generator_info, h, 4)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_generator_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def generate(self, msg_dev, batch, cw_dev, sym_dev=None, stream=None):
+        _capi.check(_capi.lib().cusat_generate(self._h, _addr(msg_dev), batch, _addr(cw_dev), _addr(sym_dev),
+                                               _stream(stream)))

@@ -66,6 +66,12 @@ _SIGS = {
     "cusat_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "cusat_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "cusat_generator_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_generator_destroy": (None, [ctypes.c_void_p]),
+    "cusat_generator_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_generate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]),
     "cusat_nms_trainer_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                  ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_nms_trainer_destroy": (None, [ctypes.c_void_p]),

@@ -19,7 +19,7 @@ import os
 
 import numpy as np
 
-from . import _capi, code_info, encode_frames, map_frames, modcod_info
+from . import _capi, code_info
 from .enums import find_modcod
 
 WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
@@ -132,45 +132,45 @@ def adopted(rows, learned_key, plain_key):
 
 
 class ChannelPool:
-    """Noisy frames of one MODCOD made on the GPU: a pool of encoded and
-    mapped codewords (unit average symbol energy), fresh AWGN per frame
-    (N0 = 1/SNR, sigma = sqrt(N0/2) per component), demapped by the
-    library's demapper with llr_gain = min(4/N0, 1000) (the conventions of
-    the reference's apps/bench_coded_modulation.cc:287-308,373-391)."""
+    """Noisy frames of one MODCOD made on the GPU: fresh random messages,
+    BCH + LDPC encoded and mapped by the library's generator (unit average
+    symbol energy), AWGN per frame (N0 = 1/SNR, sigma = sqrt(N0/2) per
+    component), demapped by the library's demapper with llr_gain =
+    min(4/N0, 1000) capped like the chain (the conventions of the reference's
+    apps/bench_coded_modulation.cc:287-308,373-391)."""
 
     def __init__(self, name, framesize, n_codewords, seed, max_batch, torch):
-        from . import demapper_cuda
+        """n_codewords is kept for callers; every draw encodes fresh messages."""
+        from . import demapper_cuda, generator
         self.torch = torch
         _, self.mod, self.rate, _, _, self.threshold = find_modcod(name)
         self.fs = framesize
         ci = code_info(framesize, self.rate)
         self.n, self.k_bch = ci["n_ldpc"], ci["k_bch"]
-        rng = np.random.default_rng(seed)
-        msg = rng.integers(0, 256, (n_codewords, self.k_bch // 8), dtype=np.uint8)
-        cw = encode_frames(framesize, self.rate, msg)
-        sym = map_frames(self.mod, self.rate, framesize, cw)
-        es = np.mean(sym.astype(np.float64)[:, 0::2] ** 2 + sym.astype(np.float64)[:, 1::2] ** 2)
-        sym = (sym * np.float32(1.0 / np.sqrt(es))).astype(np.float32)
-        self.cw = torch.from_numpy(cw).cuda()
-        self.sym = torch.from_numpy(sym).cuda()
+        self.gen_tx = generator(self.mod, self.rate, framesize, max_batch)
         self.dm = demapper_cuda(self.mod, self.rate, framesize, max_batch)
         self.max_batch = max_batch
         self.gen = torch.Generator(device="cuda")
         self.gen.manual_seed(seed)
 
     def draw(self, batch, esn0_db, stream=None):
-        """(noisy symbols, int16 LLRs, codewords) of `batch` frames, device."""
+        """(noisy symbols, int16 LLRs, codewords, N0, gain) of `batch` fresh
+        frames, device tensors."""
         torch = self.torch
+        st = stream or torch.cuda.current_stream()
         n0 = float(np.float32(1.0 / 10 ** (esn0_db / 10.0)))
         sigma = float(np.sqrt(n0 / 2.0))
-        idx = torch.randint(0, self.cw.shape[0], (batch,), device="cuda", generator=self.gen)
-        sym = self.sym[idx] + sigma * torch.randn(batch, self.sym.shape[1], device="cuda", generator=self.gen)
+        msg = torch.randint(0, 256, (batch, self.gen_tx.msg_bytes), dtype=torch.uint8, device="cuda",
+                            generator=self.gen)
+        cw = torch.empty((batch, self.gen_tx.cw_bytes), dtype=torch.uint8, device="cuda")
+        sym = torch.empty((batch, 2 * self.gen_tx.xfec), dtype=torch.float32, device="cuda")
+        self.gen_tx.generate(msg, batch, cw, sym, st)
+        sym += sigma * torch.randn(sym.shape, device="cuda", generator=self.gen)
         llr = torch.empty((batch, self.n), dtype=torch.int16, device="cuda")
         gain = min(4.0 / n0, 1000.0)
         # the fused chain caps the gain the same way (demapper_kernel.cu:283-291)
-        self.dm.demap_launch(sym, batch, n0, self.dm.capped_llr_gain(gain), llr,
-                             stream or torch.cuda.current_stream())
-        return sym, llr, self.cw[idx], n0, gain
+        self.dm.demap_launch(sym, batch, n0, self.dm.capped_llr_gain(gain), llr, st)
+        return sym, llr, cw, n0, gain
 
 
 def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128, lr=0.02, seed=1,

@@ -340,6 +340,27 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
                               uint8_t* hard_out, int32_t* trials_out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Traffic generation on the GPU                                           */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_generator cusat_generator;
+
+/* The transmitter side on the device, for generating training and benchmark
+ * traffic (reference ldpc_encode.cc, cuda/ldpc_encode_kernel.cu,
+ * cuda/bch_common.cuh with Encode = true, cuda/mapper_kernel.cu):
+ * systematic BCH encode, IRA LDPC encode and constellation mapping of a batch
+ * of messages; equal bit for bit to cusat_gen_encode and cusat_gen_map. */
+int cusat_generator_create(int modulation, int rate, int framesize, int max_batch, cusat_generator** out);
+void cusat_generator_destroy(cusat_generator* g);
+/* out[0..3] = message bytes (k_bch/8), codeword bytes (n_ldpc/8), xfecframe_len, max_batch */
+int cusat_generator_info(const cusat_generator* g, int32_t* out);
+/* msg_dev: batch x k_bch/8 bytes; cw_dev: batch x n_ldpc/8 bytes (out);
+ * sym_dev: batch x xfecframe_len complex symbols (out, or NULL); all
+ * device memory; asynchronous on `stream`. */
+int cusat_generate(cusat_generator* g, const uint8_t* msg_dev, int batch, uint8_t* cw_dev, float* sym_dev,
+                   void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Code description and traffic generation (host side; used to generate     */
 /* test and benchmark traffic, not part of the receive path)               */
 /* ---------------------------------------------------------------------- */
