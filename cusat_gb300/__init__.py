@@ -28,7 +28,7 @@ from .enums import *  # noqa: F401,F403
 from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
 
 __all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch", "server",
-           "generator",
+           "generator", "bb_extractor",
            "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
            "CusatError", "library_path"]
 
@@ -494,3 +494,27 @@ class generator:
     def generate(self, msg_dev, batch, cw_dev, sym_dev=None, stream=None):
         _capi.check(_capi.lib().cusat_generate(self._h, _addr(msg_dev), batch, _addr(cw_dev), _addr(sym_dev),
                                                _stream(stream)))
+
+
+class bb_extractor:
+    """Post-FEC baseband stage of one code: drop failed frames, descramble,
+    check the BBHEADER and pack the GSE data fields (device memory)."""
+
+    def __init__(self, framesize, rate):
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_bb_extractor_create(framesize, rate, ctypes.byref(h)))
+        self._h = h
+        self.kbch_bytes = code_info(framesize, rate)["k_bch"] // 8
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_bb_extractor_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def extract(self, hard_dev, hard_stride, trials_dev, bch_valid_dev, batch, out_dev, max_out, lengths_dev,
+                offsets_dev, stream=None):
+        _capi.check(_capi.lib().cusat_bb_extract(self._h, _addr(hard_dev), hard_stride, _addr(trials_dev),
+                                                 _addr(bch_valid_dev), batch, _addr(out_dev), max_out,
+                                                 _addr(lengths_dev), _addr(offsets_dev), _stream(stream)))

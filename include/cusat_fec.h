@@ -340,6 +340,29 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
                               uint8_t* hard_out, int32_t* trials_out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Post-FEC baseband stage                                                 */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_bb_extractor cusat_bb_extractor;
+
+/* Replaces the RX chain's host post-processing (reference
+ * rx_fec_chain.cc:604-626 with bb_scrambler.cc and bbframe_parser.cc): frames
+ * whose LDPC decode failed (trials < 0) or whose BCH check failed are dropped,
+ * the others descrambled (EN 302 307-1 5.2.2) and their BBHEADER checked
+ * (CRC-8, DFL <= 8 K_bch - 80 and a multiple of 8, TS/GS generic packetized);
+ * the DFL/8 data-field bytes of each accepted frame are packed into out_dev in
+ * frame order, a frame whose field does not fit the room left yielding
+ * nothing.  All pointers are device memory; hard_dev holds frame f's decoded
+ * bits at f * hard_stride (>= K_bch/8, e.g. the decoder's k_ldpc/8);
+ * lengths_dev[f] = bytes of frame f, offsets_dev[f] = where they start,
+ * offsets_dev[batch] = total.  Asynchronous on `stream`. */
+int cusat_bb_extractor_create(int framesize, int rate, cusat_bb_extractor** out);
+void cusat_bb_extractor_destroy(cusat_bb_extractor* x);
+int cusat_bb_extract(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_stride, const int32_t* trials_dev,
+                     const int32_t* bch_valid_dev, int batch, uint8_t* out_dev, int max_out, int32_t* lengths_dev,
+                     int32_t* offsets_dev, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Traffic generation on the GPU                                           */
 /* ---------------------------------------------------------------------- */
 

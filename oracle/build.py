@@ -22,6 +22,9 @@ REF_SOURCES = [
     "lib/cusat_dsp/modulation/bit_interleaver.cc",
     "lib/cusat_dsp/modulation/constellation.cc",
     "lib/cusat_dsp/ldpc_table_factory.cc",
+    "lib/cusat_dsp/bb_scrambler.cc",
+    "lib/cusat_dsp/bbframe_parser.cc",
+    "lib/cusat_dsp/bb_header.cc",
 ]
 
 

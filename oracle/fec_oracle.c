@@ -777,3 +777,115 @@ static int nms_edge_width(const orc_code* c)
 #include "nms_model.inc"
 #undef REAL
 #undef SFX
+
+/* ------------------------------------------------------------------------ */
+/* Post-FEC baseband stage                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* BB scrambler PRBS (EN 302 307-1 clause 5.2.2, figure 5; reference
+ * bb_scrambler.cc:18-40): 1 + X^14 + X^15, register loaded with
+ * 100101010000000 (stage 1 first) at the start of every BBFRAME, output bits
+ * MSB first. */
+void orc_bb_prbs(uint8_t* seq, int n_bytes)
+{
+    const char* init = "100101010000000";
+    unsigned reg = 0;
+    for (int s = 0; s < 15; s++)
+        if (init[s] == '1')
+            reg |= 1u << s;
+    for (int i = 0; i < n_bytes; i++) {
+        uint8_t byte = 0;
+        for (int b = 0; b < 8; b++) {
+            const unsigned out = ((reg >> 13) ^ (reg >> 14)) & 1u;
+            reg = ((reg << 1) | out) & 0x7fffu;
+            byte = (uint8_t)((byte << 1) | out);
+        }
+        seq[i] = byte;
+    }
+}
+
+/* CRC-8 of the BBHEADER (x^8 + x^7 + x^6 + x^4 + x^2 + 1, register cleared,
+ * MSB first; reference fec/crc8.h). */
+static uint8_t crc8_bb(const uint8_t* d, int n)
+{
+    uint8_t reg = 0;
+    for (int i = 0; i < n; i++) {
+        reg ^= d[i];
+        for (int b = 0; b < 8; b++)
+            reg = (reg & 0x80) ? (uint8_t)((reg << 1) ^ 0xD5) : (uint8_t)(reg << 1);
+    }
+    return reg;
+}
+
+/* The RX chain's post-FEC loop (reference rx_fec_chain.cc:604-626 with
+ * bbframe_parser.cc:14-56): a frame is used only if its LDPC decode
+ * converged and its BCH check passed; it is descrambled, its BBHEADER must
+ * have a zero CRC over its 10 bytes, DFL <= 8 kbch - 80, DFL % 8 == 0 and
+ * TS/GS = generic packetized; then its DFL/8 data-field bytes are appended
+ * to out if they fit in the room left (else the frame yields nothing).
+ * lengths[f] = bytes appended for frame f, offsets[f] = where; offsets[B] =
+ * total. */
+int orc_bb_extract(const uint8_t* hard, int stride, int kbch, const int32_t* trials, const int32_t* valid, int B,
+                   uint8_t* out, int max_out, int32_t* lengths, int32_t* offsets)
+{
+    if (kbch < 10 || kbch > 7274)
+        return -1;
+    uint8_t* prbs = (uint8_t*)malloc((size_t)kbch);
+    uint8_t* fr = (uint8_t*)malloc((size_t)kbch);
+    if (!prbs || !fr) {
+        free(prbs);
+        free(fr);
+        return -2;
+    }
+    orc_bb_prbs(prbs, kbch);
+    int used = 0;
+    for (int f = 0; f < B; f++) {
+        int n = 0;
+        offsets[f] = used;
+        if (trials[f] >= 0 && valid[f]) {
+            for (int i = 0; i < kbch; i++)
+                fr[i] = (uint8_t)(hard[(size_t)f * stride + i] ^ prbs[i]);
+            const int dfl = (fr[4] << 8) | fr[5];
+            const int ts_gs = fr[0] >> 6;
+            if (crc8_bb(fr, 10) == 0 && dfl <= 8 * kbch - 80 && dfl % 8 == 0 && ts_gs == 0) {
+                n = dfl / 8;
+                if (n > max_out - used)
+                    n = 0;
+                else
+                    memcpy(out + used, fr + 10, (size_t)n);
+            }
+        }
+        lengths[f] = n;
+        used += n;
+    }
+    offsets[B] = used;
+    free(prbs);
+    free(fr);
+    return 0;
+}
+
+/* A scrambled GSE BBFRAME of kbch bytes carrying data[0..len) (test traffic;
+ * the header layout of reference bb_header.cc:28-49: MATYPE-1 with TS/GS =
+ * matype_ts_gs, SIS = 1, CCM, roll-off 0.20; UPL = 0; DFL = 8 len; SYNC = 0;
+ * SYNCD = 0xFFFF; CRC-8), zero padding, then the PRBS. */
+int orc_bb_build(const uint8_t* data, int len, int kbch, int matype_ts_gs, uint8_t* out)
+{
+    if (len < 0 || len > kbch - 10)
+        return -1;
+    memset(out, 0, (size_t)kbch);
+    out[0] = (uint8_t)(((matype_ts_gs & 3) << 6) | 0x20 | 0x10 | 0x02);
+    out[4] = (uint8_t)((8 * len) >> 8);
+    out[5] = (uint8_t)(8 * len);
+    out[7] = 0xFF;
+    out[8] = 0xFF;
+    out[9] = crc8_bb(out, 9);
+    memcpy(out + 10, data, (size_t)len);
+    uint8_t* prbs = (uint8_t*)malloc((size_t)kbch);
+    if (!prbs)
+        return -2;
+    orc_bb_prbs(prbs, kbch);
+    for (int i = 0; i < kbch; i++)
+        out[i] ^= prbs[i];
+    free(prbs);
+    return 0;
+}

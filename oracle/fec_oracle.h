@@ -79,6 +79,15 @@ int orc_bnl_update(int raw_new, int old, int32_t* delta);
 float orc_exp_neg(float x);
 float orc_log(float x);
 
+/* Post-FEC baseband stage: the BB scrambler PRBS (n_bytes <= 7274), the
+ * RX chain's descramble + BBHEADER check + data-field extraction of a batch
+ * (hard bits of frame f at hard + f * stride, kbch bytes), and a scrambled
+ * GSE BBFRAME builder for test traffic. */
+void orc_bb_prbs(uint8_t* seq, int n_bytes);
+int orc_bb_extract(const uint8_t* hard, int stride, int kbch, const int32_t* trials, const int32_t* valid, int B,
+                   uint8_t* out, int max_out, int32_t* lengths, int32_t* offsets);
+int orc_bb_build(const uint8_t* data, int len, int kbch, int matype_ts_gs, uint8_t* out);
+
 /* Unrolled learned min-sum (training model; nms_model.inc): loss and its
  * gradient with respect to theta[T][32][2] = {beta, alpha} per iteration and
  * check degree, summed over B frames of int16 LLRs and packed codewords

@@ -12,6 +12,9 @@
 #include "modulation/bit_interleaver.h"
 #include "modulation/constellation.h"
 #include "cuda/ldpc_message_update.h"
+#include "bb_header.h"
+#include "bb_scrambler.h"
+#include "bbframe_parser.h"
 
 using namespace cusat_dsp;
 
@@ -93,4 +96,41 @@ int ref_bnl_update(int raw, int old, int32_t* delta)
     *delta = u.delta;
     return u.message;
 }
+// bb_scrambler_sequence (bb_scrambler.cc:43-49): the first n PRBS bytes
+int ref_bb_prbs(uint8_t* out, int n)
+{
+    if (n < 0 || (size_t)n > BB_SCRAMBLER_MAX_BYTES)
+        return -1;
+    memcpy(out, bb_scrambler_sequence(), (size_t)n);
+    return 0;
+}
+
+// bb_scramble (bb_scrambler.cc:53-67)
+int ref_bb_scramble(const uint8_t* in, uint8_t* out, int n)
+{
+    try {
+        bb_scramble(in, out, (size_t)n);
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// extract_gse_datafield (bbframe_parser.cc:44-56) on an already descrambled BBFRAME
+int ref_extract_datafield(const uint8_t* bbframe, int kbch, uint8_t* out, int max_out)
+{
+    return extract_gse_datafield(bbframe, (size_t)kbch, out, max_out);
+}
+
+// bb_header::build_gse_bbframe (bb_header.cc): an unscrambled GSE BBFRAME
+int ref_build_bbframe(int fs, int rate, const uint8_t* data, int len, uint8_t* out)
+{
+    try {
+        bb_header h((fecframe_size_t)fs, (code_rate_t)rate);
+        return (int)h.build_gse_bbframe(data, (unsigned)len, out);
+    } catch (...) {
+        return -1;
+    }
+}
+
 }

@@ -166,3 +166,32 @@ def nms_train(fs, rate, llr, cw, T, theta, grad=True, dtype=np.float32, nthreads
             None if iw is None else _p(iw, ct), _p(g, ct) if grad else None, _p(loss, ct), nthreads)
     assert rc == 0
     return float(loss[0]), g
+
+
+def bb_prbs(n):
+    out = np.zeros(n, np.uint8)
+    lib().orc_bb_prbs(_p(out, ctypes.c_uint8), n)
+    return out
+
+
+def bb_extract(hard, kbch, trials, valid, max_out):
+    """The RX chain's post-FEC stage over a batch: (packed data fields,
+    lengths [B], offsets [B + 1])."""
+    hard = np.ascontiguousarray(hard, np.uint8)
+    B, stride = hard.shape
+    trials = np.ascontiguousarray(trials, np.int32)
+    valid = np.ascontiguousarray(valid, np.int32)
+    out = np.zeros(max(max_out, 1), np.uint8)
+    lengths = np.zeros(B, np.int32)
+    offsets = np.zeros(B + 1, np.int32)
+    assert lib().orc_bb_extract(_p(hard, ctypes.c_uint8), stride, kbch, _p(trials, ctypes.c_int32),
+                                _p(valid, ctypes.c_int32), B, _p(out, ctypes.c_uint8), max_out,
+                                _p(lengths, ctypes.c_int32), _p(offsets, ctypes.c_int32)) == 0
+    return out[:offsets[B]], lengths, offsets
+
+
+def bb_build(data, kbch, ts_gs=0):
+    data = np.ascontiguousarray(data, np.uint8)
+    out = np.zeros(kbch, np.uint8)
+    assert lib().orc_bb_build(_p(data, ctypes.c_uint8), len(data), kbch, ts_gs, _p(out, ctypes.c_uint8)) == 0
+    return out
