@@ -145,3 +145,57 @@ def test_host_symbols(cuda, pool):
         hr, tr, vr = alone(torch, pool, e, f, T)
         assert (r.trials, r.bch_valid) == (tr, vr) and (h == hr).all()
     srv.close()
+
+
+def test_concurrent_submitters(cuda, pool):
+    """Three host threads submit interleaved traces at once; every request
+    comes back exactly once with the result it has alone."""
+    import threading
+    torch = cuda
+    T = 25
+    srv = cs.server(pool.modcods, max_trials=T, hbm_budget=128 << 20, slots=3, max_batch=32)
+    traces = [serving.make_trace(pool, 20e9, 0.0002, seed=40 + k) for k in range(3)]
+    errors = []
+
+    def submit(k):
+        try:
+            rec = serving.request_records(pool, traces[k], tag0=100000 * k)
+            serving.submit_records(srv, rec, lead_s=0.005)
+        except Exception as e:  # reported by the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=submit, args=(k,)) for k in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    total = sum(len(t) for t in traces)
+    got = []
+    while len(got) < total:
+        got += srv.poll(wait_ms=50)
+    assert len({r.tag for r in got}) == total
+    ref = {}
+    for r in got:
+        k, i = divmod(r.tag, 100000)
+        _, e, f = traces[k][i]
+        if (e, f) not in ref:
+            ref[(e, f)] = alone(torch, pool, e, f, T)
+        assert (r.trials, r.bch_valid) == ref[(e, f)][1:]
+    srv.close()
+
+
+def test_destroy_with_work_in_flight(cuda, pool):
+    """Closing a server with requests queued and batches on the GPU returns
+    promptly and leaves the device usable."""
+    import time
+    torch = cuda
+    srv = cs.server(pool.modcods, max_trials=50, hbm_budget=64 << 20, slots=2, max_batch=64)
+    serving.submit_records(srv, serving.request_records(pool, serving.make_trace(pool, 50e9, 0.002, seed=9)),
+                           lead_s=0.0)
+    time.sleep(0.005)
+    t0 = time.time()
+    srv.close()
+    assert time.time() - t0 < 10.0
+    x = torch.ones(4, device="cuda")
+    assert float((x * 2).sum().item()) == 8.0
