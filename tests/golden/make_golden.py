@@ -1,0 +1,90 @@
+"""Writes tests/golden/reference_host.json: answers of the reference's own
+host code (compiled into oracle/_ref from the reference tree by
+oracle/build.py), so that the oracle and this project's host code stay pinned
+on machines without the reference tree.
+
+    python tests/golden/make_golden.py
+
+Contents: FEC dimensions and BCH generators of every supported (frame size,
+rate); BCH codewords of seeded messages; interleaver column offsets and
+constellation points (as float32 bit patterns) of every MODCOD; the BB
+scrambler PRBS; GSE BBFRAMEs built by the reference and its data-field
+extraction of them."""
+import ctypes
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle_lib as O  # noqa: E402
+from cusat_gb300 import enums as E  # noqa: E402
+
+
+def p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def main():
+    ref = O.ref()
+    if ref is None:
+        raise SystemExit("the reference tree is needed to generate the fixtures")
+    doc = {"codes": [], "bch_words": [], "modcods": [], "bbframes": []}
+    for fs in (0, 1):
+        for r in range(E.RATE_COUNT):
+            out = np.zeros(5, np.uint32)
+            if ref.ref_fec_params(fs, r, p(out)) != 0:
+                continue
+            k_bch, n_bch, t, k_ldpc, n_ldpc = (int(v) for v in out)
+            gen = np.zeros(4, np.uint64)
+            deg = ref.ref_bch_generator(fs, n_bch, t, p(gen))
+            doc["codes"].append({"fs": fs, "rate": r, "k_bch": k_bch, "n_bch": n_bch, "t": t, "k_ldpc": k_ldpc,
+                                 "n_ldpc": n_ldpc, "bch_degree": deg, "bch_gen": [str(int(g)) for g in gen]})
+    for fs, r in [(0, E.RATE_3_5), (0, E.RATE_1_4), (0, E.RATE_9_10), (1, E.RATE_1_2), (1, E.RATE_8_9)]:
+        c = next(c for c in doc["codes"] if (c["fs"], c["rate"]) == (fs, r))
+        rng = np.random.default_rng(1000 + 10 * fs + r)
+        msg = rng.integers(0, 256, c["k_bch"] // 8, dtype=np.uint8)
+        cw = np.zeros(c["n_bch"] // 8, np.uint8)
+        ref.ref_bch_encode(fs, c["n_bch"], c["t"], p(msg), p(cw))
+        doc["bch_words"].append({"fs": fs, "rate": r, "msg_seed": 1000 + 10 * fs + r, "parity": cw[len(msg):].tobytes().hex()})
+    for m in E.MODCODS:
+        for fs in (0, 1):
+            re = np.zeros(256, np.float32)
+            im = np.zeros(256, np.float32)
+            bits = ref.ref_constellation(m[1], m[2], fs, p(re), p(im))
+            if bits <= 0:
+                continue
+            col = np.zeros(8, np.uint32)
+            rows = np.zeros(1, np.uint32)
+            ncol = ref.ref_interleaver(m[1], m[2], fs, p(col), p(rows))
+            n = 1 << bits
+            doc["modcods"].append({"name": m[3], "fs": fs, "bits": bits, "n_cols": int(ncol),
+                                   "col": [int(v) for v in col], "re": re[:n].view(np.uint32).tolist(),
+                                   "im": im[:n].view(np.uint32).tolist()})
+    prbs = np.zeros(7274, np.uint8)
+    ref.ref_bb_prbs(p(prbs), 7274)
+    doc["prbs_head"] = prbs[:64].tobytes().hex()
+    doc["prbs_sha256"] = hashlib.sha256(prbs.tobytes()).hexdigest()
+    for fs, r, n, seed in [(0, E.RATE_3_5, 100, 1), (1, E.RATE_1_2, 0, 2), (1, E.RATE_1_2, 869, 3)]:
+        c = next(c for c in doc["codes"] if (c["fs"], c["rate"]) == (fs, r))
+        kbch = c["k_bch"] // 8
+        data = np.random.default_rng(seed).integers(0, 256, n, dtype=np.uint8)
+        plain = np.zeros(kbch, np.uint8)
+        ref.ref_build_bbframe(fs, r, p(data), n, p(plain))
+        outb = np.zeros(kbch, np.uint8)
+        got = ref.ref_extract_datafield(p(plain), kbch, p(outb), kbch)
+        doc["bbframes"].append({"fs": fs, "rate": r, "payload_seed": seed, "len": n,
+                                "header": plain[:10].tobytes().hex(), "extracted": int(got)})
+    path = os.path.join(HERE, "reference_host.json")
+    with open(path, "w") as f:
+        json.dump(doc, f, separators=(",", ":"))
+    print(path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()
