@@ -343,9 +343,16 @@ __device__ __forceinline__ void complete_groups(unsigned char* smem, const int16
         const uint2 it = t.items[k];
         const int r0 = (int)(it.y & 0xff), nr = (int)(it.y >> 8);
         const int app = lds16(smem, (int)it.x + 2 * j);
-        int sum = app;
-        for (int g = 0; g < nr; g++)
-            sum += SAT ? (int)st[(r0 + g) * kM + j] : (int)st[(r0 + g) * kM + j] - app;
+        const int16_t* rows = st + r0 * kM + j;
+        int sum;
+        if (!SAT && nr == 2) {
+            // the common group of two writers: row0 + row1 - APP
+            sum = (int)rows[0] + (int)rows[kM] - app;
+        } else {
+            sum = app;
+            for (int g = 0; g < nr; g++)
+                sum += SAT ? (int)rows[g * kM] : (int)rows[g * kM] - app;
+        }
         sts16(smem, (int)it.x + 2 * j, SAT ? sat16(sum) : sum);
     }
 }
