@@ -11,6 +11,10 @@ arguments and result conventions of the reference's C++ classes for the path:
   demapper_cuda     lib/cusat_dsp/cuda/demapper_kernel.cuh:23-89
   bch_check_cuda    lib/cusat_dsp/cuda/bch_check_kernel.cuh:9-24
 
+  rx_fec_chain      lib/cusat_dsp/rx_fec_chain.h:61-297
+  rx_fec_pool       lib/cusat_dsp/rx_fec_pool.h:25-140
+  gpu_decode_budget lib/cusat_dsp/rx_fec_chain.h:52-59
+
 plus ``rx_fec`` (one MODCOD's fused demap -> decode -> BCH chain).
 
 Device buffers are torch CUDA tensors (or raw device addresses as int);
@@ -28,7 +32,7 @@ from .enums import *  # noqa: F401,F403
 from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
 
 __all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch", "server",
-           "generator", "bb_extractor",
+           "generator", "bb_extractor", "gpu_decode_budget", "rx_fec_chain", "rx_fec_pool", "dd_snr",
            "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
            "CusatError", "library_path"]
 
@@ -518,3 +522,283 @@ class bb_extractor:
         _capi.check(_capi.lib().cusat_bb_extract(self._h, _addr(hard_dev), hard_stride, _addr(trials_dev),
                                                  _addr(bch_valid_dev), batch, _addr(out_dev), max_out,
                                                  _addr(lengths_dev), _addr(offsets_dev), _stream(stream)))
+
+
+def _symbols(symbols):
+    """Host symbols as a contiguous float32 (re, im) array and their count."""
+    a = np.asarray(symbols)
+    if np.iscomplexobj(a):
+        a = np.ascontiguousarray(a, np.complex64).view(np.float32)
+    else:
+        a = np.ascontiguousarray(a, np.float32)
+    return a, a.size // 2
+
+
+def dd_snr(constellation, rate, framesize, symbols, stride=1):
+    """Decision-directed SNR (linear) of host symbols: qpsk_snr_dd for QPSK,
+    constellation_snr_dd on every stride-th symbol otherwise."""
+    a, n = _symbols(symbols)
+    out = ctypes.c_float()
+    _capi.check(_capi.lib().cusat_dd_snr(constellation, rate, framesize, a.ctypes.data, n, stride,
+                                         ctypes.byref(out)))
+    return out.value
+
+
+class gpu_decode_budget:
+    """Shared cap on frames in flight across chains (0 = unlimited)."""
+
+    def __init__(self, cap=-1):
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_decode_budget_create(cap, ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def make_default(cls):
+        return cls(-1)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_decode_budget_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    @property
+    def cap(self):
+        return _info(_capi.lib().cusat_decode_budget_info, self._h, 2)[0]
+
+    @property
+    def in_flight(self):
+        return _info(_capi.lib().cusat_decode_budget_info, self._h, 2)[1]
+
+
+def _check_ready(rc):
+    if rc < 0:
+        _capi.check(rc)
+    return rc > 0
+
+
+class rx_fec_chain:
+    """One MODCOD's frame-at-a-time receive chain: submit XFECFRAMEs, drain
+    completed micro-batches in order, read the GSE data fields."""
+
+    def __init__(self, framesize, rate, constellation, max_trials=25, cuda_max_batch=64, n_gpu_streams=8,
+                 micro_batch=4, _handle=None):
+        self._owned = _handle is None
+        if _handle is None:
+            h = ctypes.c_void_p()
+            _capi.check(_capi.lib().cusat_rx_chain_create(framesize, rate, constellation, max_trials,
+                                                          cuda_max_batch, n_gpu_streams, micro_batch,
+                                                          ctypes.byref(h)))
+            _handle = h
+        self._h = _handle
+        info = _info(_capi.lib().cusat_rx_chain_info, self._h, 6)
+        self.xfecframe_len, self.kbch_bytes, self._batch_size, self._max_out, self.micro_batch, self.n_streams = info
+        self._budget = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            if self._owned:
+                _capi.lib().cusat_rx_chain_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    @staticmethod
+    def frame_passes_fec_checks(ldpc_trials_remaining, bch_valid):
+        return ldpc_trials_remaining >= 0 and bool(bch_valid)
+
+    def submit_xfecframe(self, symbols, n_symbols=None):
+        a, n = _symbols(symbols)
+        if n_symbols is not None:
+            n = min(n, int(n_symbols))
+        return _check_ready(_capi.lib().cusat_rx_chain_submit_xfecframe(self._h, a.ctypes.data, n))
+
+    def drain_completed(self):
+        return _check_ready(_capi.lib().cusat_rx_chain_drain_completed(self._h))
+
+    def get_gse_output(self, max_bytes=None):
+        if max_bytes is None:
+            max_bytes = self._max_out
+        out = np.empty(max(max_bytes, 1), np.uint8)
+        n = _capi.lib().cusat_rx_chain_get_gse_output(self._h, out.ctypes.data, max_bytes)
+        if n < 0:
+            _capi.check(n)
+        return out[:n].copy()
+
+    def gse_dfl_sizes(self):
+        n = _capi.lib().cusat_rx_chain_gse_dfl_sizes(self._h, None, 0)
+        if n < 0:
+            _capi.check(n)
+        out = np.zeros(max(n, 1), np.int32)
+        _capi.lib().cusat_rx_chain_gse_dfl_sizes(self._h, out.ctypes.data, n)
+        return [int(v) for v in out[:n]]
+
+    def launch_partial(self):
+        _capi.check(_capi.lib().cusat_rx_chain_launch_partial(self._h))
+
+    def flush(self):
+        _capi.check(_capi.lib().cusat_rx_chain_flush(self._h))
+
+    def reset(self):
+        _capi.check(_capi.lib().cusat_rx_chain_reset(self._h))
+
+    def warmup(self):
+        _capi.check(_capi.lib().cusat_rx_chain_warmup(self._h))
+
+    def update_snr(self, snr_db):
+        _capi.lib().cusat_rx_chain_update_snr(self._h, snr_db)
+
+    def set_block_when_full(self, on):
+        _capi.lib().cusat_rx_chain_set_block_when_full(self._h, 1 if on else 0)
+
+    def set_decode_budget(self, budget):
+        if budget is not None:
+            _capi.check(_capi.lib().cusat_rx_chain_set_decode_budget(self._h, budget._h))
+            self._budget = budget
+
+    def set_weights(self, weights):
+        w, n = _weights_arg(weights)
+        _capi.check(_capi.lib().cusat_rx_chain_set_weights(self._h, w, n))
+
+    def _stats(self):
+        out = np.zeros(12, np.float64)
+        _capi.check(_capi.lib().cusat_rx_chain_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def frame_count(self):
+        return int(self._stats()[0])
+
+    def frame_error_count(self):
+        return int(self._stats()[1])
+
+    def gpu_drop_count(self):
+        return int(self._stats()[2])
+
+    def gpu_inflight(self):
+        return int(self._stats()[3])
+
+    def gpu_pending_launch(self):
+        return int(self._stats()[4])
+
+    def force_drain_count(self):
+        return int(self._stats()[5])
+
+    def pending_count(self):
+        return int(self._stats()[6])
+
+    def snr_db(self):
+        return float(self._stats()[7])
+
+    data_snr_db = snr_db
+
+    def precision(self):
+        return float(self._stats()[8])
+
+    def noise_var(self):
+        return float(self._stats()[9])
+
+    def batch_age_s(self):
+        return float(self._stats()[10])
+
+    def batch_size(self):
+        return self._batch_size
+
+    def max_output_bytes(self):
+        return self._max_out
+
+
+class rx_fec_pool:
+    """One rx_fec_chain per enabled MODCOD (modcod_idx values of the MODCOD
+    table) behind one decode budget; output blocks in submission order."""
+
+    def __init__(self, framesize, enabled_modcods, max_trials=25, cuda_max_batch=64, n_gpu_streams=8,
+                 micro_batch=4):
+        from .enums import modcod_by_index
+        triples = []
+        for idx in enabled_modcods:
+            m = modcod_by_index(int(idx))
+            triples += [m[0], m[1], m[2]]
+        arr = np.asarray(triples, np.int32)
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_rx_pool_create(framesize, arr.ctypes.data, len(enabled_modcods), max_trials,
+                                                     cuda_max_batch, n_gpu_streams, micro_batch, ctypes.byref(h)))
+        self._h = h
+        self.modcods = [int(i) for i in enabled_modcods]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_rx_pool_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def chain(self, modcod):
+        h = _capi.lib().cusat_rx_pool_chain(self._h, modcod)
+        return rx_fec_chain(0, 0, 0, _handle=ctypes.c_void_p(h)) if h else None
+
+    def submit(self, symbols, modcod, n_symbols=None):
+        a, n = _symbols(symbols)
+        if n_symbols is not None:
+            n = min(n, int(n_symbols))
+        return _check_ready(_capi.lib().cusat_rx_pool_submit(self._h, a.ctypes.data, n, modcod))
+
+    def get_gse_output(self, max_bytes=None):
+        if max_bytes is None:
+            max_bytes = self.max_output_bytes()
+        out = np.empty(max(max_bytes, 1), np.uint8)
+        n = _capi.lib().cusat_rx_pool_get_gse_output(self._h, out.ctypes.data, max_bytes)
+        if n < 0:
+            _capi.check(n)
+        return out[:n].copy()
+
+    def gse_dfl_sizes(self):
+        n = _capi.lib().cusat_rx_pool_gse_dfl_sizes(self._h, None, 0)
+        out = np.zeros(max(n, 1), np.int32)
+        _capi.lib().cusat_rx_pool_gse_dfl_sizes(self._h, out.ctypes.data, n)
+        return [int(v) for v in out[:n]]
+
+    def drain_all_completed(self):
+        return _check_ready(_capi.lib().cusat_rx_pool_drain_all_completed(self._h))
+
+    def finish_all_pending(self):
+        _capi.check(_capi.lib().cusat_rx_pool_finish_all_pending(self._h))
+
+    def launch_stale(self, max_age_ms):
+        return _check_ready(_capi.lib().cusat_rx_pool_launch_stale(self._h, float(max_age_ms)))
+
+    def reset_all(self):
+        _capi.check(_capi.lib().cusat_rx_pool_reset_all(self._h))
+
+    def warmup_all(self):
+        _capi.check(_capi.lib().cusat_rx_pool_warmup_all(self._h))
+
+    def update_snr(self, modcod, snr_db):
+        _capi.lib().cusat_rx_pool_update_snr(self._h, modcod, snr_db)
+
+    def _stats(self):
+        out = np.zeros(5, np.float64)
+        _capi.check(_capi.lib().cusat_rx_pool_stats(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def total_frame_count(self):
+        return int(self._stats()[0])
+
+    def total_error_count(self):
+        return int(self._stats()[1])
+
+    def total_gpu_drop_count(self):
+        return int(self._stats()[2])
+
+    def max_output_bytes(self):
+        return int(self._stats()[3])
+
+    def data_snr_db(self):
+        return float(self._stats()[4])
+
+    def modcod_counters(self, modcod):
+        f, e = ctypes.c_uint64(), ctypes.c_uint64()
+        rc = _capi.lib().cusat_rx_pool_modcod_counters(self._h, modcod, ctypes.byref(f), ctypes.byref(e))
+        if rc < 0:
+            _capi.check(rc)
+        return (int(f.value), int(e.value)) if rc == 1 else None

@@ -97,6 +97,49 @@ _SIGS = {
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),
     "cusat_batch_capture": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "cusat_batch_replay": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cusat_decode_budget_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_decode_budget_destroy": (None, [ctypes.c_void_p]),
+    "cusat_decode_budget_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_dd_snr": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                    ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "cusat_rx_chain_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_rx_chain_destroy": (None, [ctypes.c_void_p]),
+    "cusat_rx_chain_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
+    "cusat_rx_chain_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_chain_set_decode_budget": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cusat_rx_chain_set_launch_lock": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                      ctypes.c_void_p]),
+    "cusat_rx_chain_set_block_when_full": (None, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_chain_update_snr": (None, [ctypes.c_void_p, ctypes.c_float]),
+    "cusat_rx_chain_submit_xfecframe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_chain_drain_completed": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_chain_get_gse_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_chain_gse_dfl_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_chain_launch_partial": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_chain_flush": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_chain_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_chain_warmup": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_chain_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "cusat_rx_pool_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_rx_pool_destroy": (None, [ctypes.c_void_p]),
+    "cusat_rx_pool_chain": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_pool_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "cusat_rx_pool_get_gse_output": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_pool_gse_dfl_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_pool_drain_all_completed": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_pool_finish_all_pending": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_pool_launch_stale": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "cusat_rx_pool_reset_all": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_pool_warmup_all": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_rx_pool_update_snr": (None, [ctypes.c_void_p, ctypes.c_int, ctypes.c_float]),
+    "cusat_rx_pool_set_launch_lock": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p]),
+    "cusat_rx_pool_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "cusat_rx_pool_modcod_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
+                                                     ctypes.POINTER(ctypes.c_uint64),
+                                                     ctypes.POINTER(ctypes.c_uint64)]),
     "cusat_code_info": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_int_p]),
     "cusat_gen_encode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int]),

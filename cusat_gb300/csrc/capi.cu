@@ -79,7 +79,9 @@ struct Engine {
            "occupancy");
         if (per_sm < 1)
             return fail(CUSAT_ERR_UNSUPPORTED, "decoder kernel cannot be resident");
-        grid_max = per_sm * sms;
+        // no launch runs more CTAs than frames: message scratch for at most
+        // max_batch of them
+        grid_max = per_sm * sms < batch ? per_sm * sms : batch;
         const size_t msg_bytes = (size_t)grid_max * p->R * p->msg_row;
         CU(cudaMalloc(&msg, msg_bytes), "cudaMalloc(messages)");
         CU(cudaMalloc(&queue, 256), "cudaMalloc(queue)");

@@ -75,6 +75,12 @@ int make_constellation(int modulation, int rate, int framesize, std::vector<floa
 // Interleaver: column offsets; returns the number of columns (0 = none).
 int make_interleaver(int modulation, int rate, int framesize, uint32_t col[8], uint32_t* rows);
 
+// Decision-directed SNR estimates (linear) of received symbols (re, im):
+// QPSK by the signs, any constellation by its nearest point on every
+// stride-th symbol.
+float dd_snr_qpsk(const float* sym, int n_sym);
+float dd_snr_points(const std::vector<float>& pts, const float* sym, int n_sym, int stride);
+
 // Product-side encoders used to generate test traffic (bench, training).
 void bch_encode_frames(const CodePlan& c, const uint8_t* msg, uint8_t* cw, int B);
 void ldpc_encode_frames(const CodePlan& c, const uint8_t* info, uint8_t* cw, int B);

@@ -8,6 +8,8 @@
 // the reference's (checked against the reference host code in the tests).
 // 128APSK and the coordinate-table 256APSK rates are not built here.
 #include <math.h>
+
+#include <cmath>
 #include <string.h>
 
 #include <algorithm>
@@ -476,6 +478,59 @@ void map_frames(const ModcodDemap& d, const uint8_t* cw, int B, float* sym)
             out[2 * j + 1] = d.pts[2 * label + 1];
         }
     }
+}
+
+// Decision-directed SNR (reference modulation/dd_snr.cc:12-47): each symbol
+// is replaced by its nearest constellation point; SNR = energy of the
+// decisions / energy of the errors, 1e6 when the errors are that small, 0 for
+// non-finite input.  Float accumulation in symbol order, no contraction (this
+// file is built with -ffp-contract=off), so the value is the reference's.
+static float dd_ratio(float signal, float error)
+{
+    if (!std::isfinite(signal) || !std::isfinite(error))
+        return 0.0f;
+    const float cap = 1e6f;
+    return error * cap <= signal ? cap : signal / error;
+}
+
+float dd_snr_qpsk(const float* sym, int n_sym)
+{
+    const float a = (float)0.70710678118654752440;
+    float signal = 0.0f, error = 0.0f;
+    for (int i = 0; i < n_sym; i++) {
+        const float re = sym[2 * i], im = sym[2 * i + 1];
+        const float dr = re < 0 ? -a : a, di = im < 0 ? -a : a;
+        signal += dr * dr + di * di;
+        const float er = re - dr, ei = im - di;
+        error += er * er;
+        error += ei * ei;
+    }
+    return dd_ratio(signal, error);
+}
+
+float dd_snr_points(const std::vector<float>& pts, const float* sym, int n_sym, int stride)
+{
+    const int n_points = (int)pts.size() / 2;
+    float signal = 0.0f, error = 0.0f;
+    for (int i = 0; i < n_sym; i += stride) {
+        const float re = sym[2 * i], im = sym[2 * i + 1];
+        // nearest point, first of equals (reference constellation.cc:495-507)
+        int best = 0;
+        float best_d = 3.402823466e38f;
+        for (int l = 0; l < n_points; l++) {
+            const float dr = re - pts[2 * l], di = im - pts[2 * l + 1];
+            const float d = dr * dr + di * di;
+            if (d < best_d) {
+                best_d = d;
+                best = l;
+            }
+        }
+        const float pr = pts[2 * best], pi = pts[2 * best + 1];
+        signal += pr * pr + pi * pi;
+        const float er = re - pr, ei = im - pi;
+        error += er * er + ei * ei;
+    }
+    return dd_ratio(signal, error);
 }
 
 }  // namespace cusat

@@ -75,3 +75,11 @@ def find_modcod(name):
         if m[3] == name:
             return m
     raise KeyError(name)
+
+
+def modcod_by_index(idx):
+    """The MODCOD table row of a modcod_idx (acm_config.h find_modcod)."""
+    for m in MODCODS:
+        if m[0] == idx:
+            return m
+    raise KeyError(idx)

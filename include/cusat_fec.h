@@ -363,6 +363,98 @@ int cusat_bb_extract(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_st
                      int32_t* offsets_dev, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Frame-at-a-time receive chain and per-MODCOD pool                       */
+/* ---------------------------------------------------------------------- */
+
+/* Shared in-flight budget of decode blocks (frames), replacing
+ * cusat_dsp::gpu_decode_budget (lib/cusat_dsp/rx_fec_chain.h:52-59).
+ * cap < 0: the default, one frame per SM, overridden by the environment
+ * variable CUSAT_LDPC_INFLIGHT_CAP; cap 0: unlimited.  Chains keep their
+ * share alive after the handle is destroyed.  info: out[0] = cap,
+ * out[1] = frames in flight. */
+typedef struct cusat_decode_budget cusat_decode_budget;
+int cusat_decode_budget_create(int cap, cusat_decode_budget** out);
+void cusat_decode_budget_destroy(cusat_decode_budget* b);
+int cusat_decode_budget_info(const cusat_decode_budget* b, int32_t* out);
+
+/* Decision-directed SNR (linear) of n_sym symbols (re, im): QPSK by the
+ * signs, other constellations by the nearest point on every stride-th
+ * symbol.  Replaces qpsk_snr_dd / constellation_snr_dd
+ * (lib/cusat_dsp/modulation/dd_snr.h:17-21). */
+int cusat_dd_snr(int modulation, int rate, int framesize, const float* sym, int n_sym, int stride, float* out);
+
+/* One MODCOD's frame-at-a-time receive chain, replacing cusat_dsp::rx_fec_chain
+ * (lib/cusat_dsp/rx_fec_chain.h:61-297) call for call: frames accumulate
+ * into micro-batches in a 128-slot flight ring, each full micro-batch is
+ * launched at once (within the decode budget) on the next of n_gpu_streams
+ * streams, completed slots are drained in submission order into GSE output
+ * (the data fields of frames that converged, passed BCH and carry a valid
+ * GSE BBHEADER) and per-frame data-field sizes.  Every 32nd submitted frame
+ * re-estimates the SNR (decision-directed; pilot SNR for >= 128 points).
+ * Return conventions: submit / drain return 1 when output is available,
+ * 0 when not, < 0 on error (the reference aborts); a frame of the wrong
+ * length or one that finds the ring full is counted as dropped and as a
+ * frame error, as in the reference.  Not thread-safe (like the reference);
+ * the launch lock (rx_fec_chain::set_cuda_mutex) serialises the chain's CUDA
+ * launches with the caller's. */
+typedef struct cusat_rx_chain cusat_rx_chain;
+int cusat_rx_chain_create(int framesize, int rate, int modulation, int max_trials, int cuda_max_batch,
+                          int n_gpu_streams, int micro_batch, cusat_rx_chain** out);
+void cusat_rx_chain_destroy(cusat_rx_chain* c);
+/* out[0..5] = xfecframe_len, kbch_bytes, batch_size(), max_output_bytes(),
+ * micro_batch, streams */
+int cusat_rx_chain_info(const cusat_rx_chain* c, int32_t* out);
+int cusat_rx_chain_set_weights(cusat_rx_chain* c, const int16_t* weights, int n_iter);
+int cusat_rx_chain_set_decode_budget(cusat_rx_chain* c, const cusat_decode_budget* b);
+int cusat_rx_chain_set_launch_lock(cusat_rx_chain* c, void (*lock)(void*), void (*unlock)(void*), void* ctx);
+void cusat_rx_chain_set_block_when_full(cusat_rx_chain* c, int on);
+void cusat_rx_chain_update_snr(cusat_rx_chain* c, float snr_db);
+/* symbols: n_symbols complex (re, im) host values; copied before return */
+int cusat_rx_chain_submit_xfecframe(cusat_rx_chain* c, const float* symbols, int n_symbols);
+int cusat_rx_chain_drain_completed(cusat_rx_chain* c);
+int cusat_rx_chain_get_gse_output(cusat_rx_chain* c, uint8_t* out, int max_bytes);
+/* returns the number of sizes; copies up to max of them */
+int cusat_rx_chain_gse_dfl_sizes(const cusat_rx_chain* c, int32_t* out, int max);
+int cusat_rx_chain_launch_partial(cusat_rx_chain* c);
+int cusat_rx_chain_flush(cusat_rx_chain* c);
+int cusat_rx_chain_reset(cusat_rx_chain* c);
+int cusat_rx_chain_warmup(cusat_rx_chain* c);
+/* out[0..11] = frame_count, frame_error_count, gpu_drop_count, gpu_inflight
+ * (slots), gpu_pending_launch, force_drain_count, pending_count, snr_db,
+ * precision (LLR gain), noise variance, age of the partial micro-batch (s),
+ * output bytes waiting */
+int cusat_rx_chain_stats(const cusat_rx_chain* c, double* out);
+
+/* One chain per enabled MODCOD behind one decode budget, replacing
+ * cusat_dsp::rx_fec_pool (lib/cusat_dsp/rx_fec_pool.h:25-140).  modcods:
+ * n triples (modcod_idx, modulation, rate), the caller's find_modcod()
+ * lookup.  A MODCOD change flushes the previous MODCOD's chain before the new
+ * frame is admitted, so output blocks come out in submission order;
+ * submit of a MODCOD not enabled is skipped (returns 0).  Chains are visited
+ * in creation order. */
+typedef struct cusat_rx_pool cusat_rx_pool;
+int cusat_rx_pool_create(int framesize, const int32_t* modcods, int n_modcods, int max_trials, int cuda_max_batch,
+                         int n_gpu_streams, int micro_batch, cusat_rx_pool** out);
+void cusat_rx_pool_destroy(cusat_rx_pool* p);
+/* the pool's chain of one MODCOD (owned by the pool), or NULL */
+cusat_rx_chain* cusat_rx_pool_chain(cusat_rx_pool* p, int modcod);
+int cusat_rx_pool_submit(cusat_rx_pool* p, const float* symbols, int n_symbols, int modcod);
+int cusat_rx_pool_get_gse_output(cusat_rx_pool* p, uint8_t* out, int max_bytes);
+int cusat_rx_pool_gse_dfl_sizes(const cusat_rx_pool* p, int32_t* out, int max);
+int cusat_rx_pool_drain_all_completed(cusat_rx_pool* p);
+int cusat_rx_pool_finish_all_pending(cusat_rx_pool* p);
+int cusat_rx_pool_launch_stale(cusat_rx_pool* p, double max_age_ms);
+int cusat_rx_pool_reset_all(cusat_rx_pool* p);
+int cusat_rx_pool_warmup_all(cusat_rx_pool* p);
+void cusat_rx_pool_update_snr(cusat_rx_pool* p, int modcod, float snr_db);
+int cusat_rx_pool_set_launch_lock(cusat_rx_pool* p, void (*lock)(void*), void (*unlock)(void*), void* ctx);
+/* out[0..4] = total frames, total errors, total GPU drops, max_output_bytes,
+ * data SNR (dB) of the last decoded MODCOD */
+int cusat_rx_pool_stats(const cusat_rx_pool* p, double* out);
+/* 1 and the counters if the MODCOD is enabled, else 0 */
+int cusat_rx_pool_modcod_counters(const cusat_rx_pool* p, int modcod, uint64_t* frames, uint64_t* errors);
+
+/* ---------------------------------------------------------------------- */
 /* Traffic generation on the GPU                                           */
 /* ---------------------------------------------------------------------- */
 

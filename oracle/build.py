@@ -25,6 +25,7 @@ REF_SOURCES = [
     "lib/cusat_dsp/bb_scrambler.cc",
     "lib/cusat_dsp/bbframe_parser.cc",
     "lib/cusat_dsp/bb_header.cc",
+    "lib/cusat_dsp/modulation/dd_snr.cc",
 ]
 
 

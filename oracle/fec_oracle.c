@@ -7,6 +7,7 @@
  */
 #include "fec_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -888,4 +889,46 @@ int orc_bb_build(const uint8_t* data, int len, int kbch, int matype_ts_gs, uint8
         out[i] ^= prbs[i];
     free(prbs);
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Decision-directed SNR estimate (reference modulation/dd_snr.cc:12-47 and  */
+/* nearest_label, modulation/constellation.cc:495-507)                       */
+/* ------------------------------------------------------------------------ */
+
+float orc_dd_snr(const float* sym, int n_sym, const float* pts, int n_points, int stride, int qpsk)
+{
+    float sig = 0.0f, err = 0.0f;
+    if (qpsk) {
+        const float h = 0.70710678f;
+        for (int i = 0; i < n_sym; i++) {
+            float x = sym[2 * i], y = sym[2 * i + 1];
+            float a = x < 0 ? -h : h, b = y < 0 ? -h : h;
+            float ex = x - a, ey = y - b;
+            sig += a * a + b * b;
+            err += ex * ex;
+            err += ey * ey;
+        }
+    } else {
+        for (int i = 0; i < n_sym; i += stride) {
+            float x = sym[2 * i], y = sym[2 * i + 1];
+            int k = 0;
+            float dk = FLT_MAX;
+            for (int l = 0; l < n_points; l++) {
+                float u = x - pts[2 * l], v = y - pts[2 * l + 1];
+                float d = u * u + v * v;
+                if (d < dk) {
+                    dk = d;
+                    k = l;
+                }
+            }
+            float px = pts[2 * k], py = pts[2 * k + 1];
+            float ex = x - px, ey = y - py;
+            sig += px * px + py * py;
+            err += ex * ex + ey * ey;
+        }
+    }
+    if (!isfinite(sig) || !isfinite(err))
+        return 0.0f;
+    return err * 1e6f <= sig ? 1e6f : sig / err;
 }

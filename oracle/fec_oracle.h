@@ -88,6 +88,11 @@ int orc_bb_extract(const uint8_t* hard, int stride, int kbch, const int32_t* tri
                    uint8_t* out, int max_out, int32_t* lengths, int32_t* offsets);
 int orc_bb_build(const uint8_t* data, int len, int kbch, int matype_ts_gs, uint8_t* out);
 
+/* Decision-directed SNR (linear) of n_sym symbols (re, im): QPSK by the
+ * signs of I and Q (qpsk != 0), otherwise the nearest of n_points points on
+ * every stride-th symbol.  Reference modulation/dd_snr.cc:12-47. */
+float orc_dd_snr(const float* sym, int n_sym, const float* pts, int n_points, int stride, int qpsk);
+
 /* Unrolled learned min-sum (training model; nms_model.inc): loss and its
  * gradient with respect to theta[T][32][2] = {beta, alpha} per iteration and
  * check degree, summed over B frames of int16 LLRs and packed codewords

@@ -11,6 +11,7 @@
 #include "ldpc_table_factory.h"
 #include "modulation/bit_interleaver.h"
 #include "modulation/constellation.h"
+#include "modulation/dd_snr.h"
 #include "cuda/ldpc_message_update.h"
 #include "bb_header.h"
 #include "bb_scrambler.h"
@@ -59,6 +60,16 @@ int ref_interleaver(int mod, int rate, int fs, uint32_t* col8, uint32_t* rows)
     } catch (...) {
         return -1;
     }
+}
+
+// qpsk_snr_dd / constellation_snr_dd (modulation/dd_snr.cc:23-47)
+float ref_dd_snr(int mod, int rate, int fs, const float* sym, int n_sym, int stride, int qpsk)
+{
+    const complexf* z = reinterpret_cast<const complexf*>(sym);
+    if (qpsk)
+        return qpsk_snr_dd(z, n_sym);
+    constellation_t c = make_constellation((modulation_t)mod, (code_rate_t)rate, (fecframe_size_t)fs);
+    return constellation_snr_dd(c, z, n_sym, stride);
 }
 
 // make_constellation (modulation/constellation.cc:461-496): points by label

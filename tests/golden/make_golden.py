@@ -9,7 +9,7 @@ Contents: FEC dimensions and BCH generators of every supported (frame size,
 rate); BCH codewords of seeded messages; interleaver column offsets and
 constellation points (as float32 bit patterns) of every MODCOD; the BB
 scrambler PRBS; GSE BBFRAMEs built by the reference and its data-field
-extraction of them."""
+extraction of them; decision-directed SNR estimates of seeded symbols."""
 import ctypes
 import hashlib
 import json
@@ -28,6 +28,21 @@ from cusat_gb300 import enums as E  # noqa: E402
 
 def p(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+# (modulation, rate, frame size, stride, seed) of the SNR-estimate vectors
+DD_CASES = [(0, 3, 1, 1, 21), (1, 4, 0, 8, 22), (1, 4, 0, 1, 23), (3, 6, 0, 8, 24), (4, 6, 0, 8, 25),
+            (3, 6, 0, 1, 26)]
+
+
+def dd_symbols(seed, n=2000):
+    """Seeded symbols for the SNR vectors: uniform over [-1.3, 1.3)^2, and for
+    seed 0 exact QPSK points (zero decision error)."""
+    if seed == 0:
+        a = np.float32(np.sqrt(0.5))
+        s = np.random.default_rng(7).integers(0, 2, 2 * n) * 2 - 1
+        return (s * a).astype(np.float32)
+    return np.random.default_rng(seed).uniform(-1.3, 1.3, 2 * n).astype(np.float32)
 
 
 def main():
@@ -80,6 +95,12 @@ def main():
         got = ref.ref_extract_datafield(p(plain), kbch, p(outb), kbch)
         doc["bbframes"].append({"fs": fs, "rate": r, "payload_seed": seed, "len": n,
                                 "header": plain[:10].tobytes().hex(), "extracted": int(got)})
+    doc["dd_snr"] = []
+    for mod, rate, fs, stride, seed in DD_CASES + [(0, 3, 1, 1, 0)]:
+        sym = dd_symbols(seed)
+        v = ref.ref_dd_snr(mod, rate, fs, p(sym), len(sym) // 2, stride, 1 if mod == 0 else 0)
+        doc["dd_snr"].append({"mod": mod, "rate": rate, "fs": fs, "stride": stride, "seed": seed,
+                              "value": int(np.float32(v).view(np.uint32))})
     path = os.path.join(HERE, "reference_host.json")
     with open(path, "w") as f:
         json.dump(doc, f, separators=(",", ":"))

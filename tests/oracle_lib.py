@@ -30,6 +30,7 @@ def lib():
         _lib.orc_exp_neg.argtypes = [ctypes.c_float]
         _lib.orc_log.restype = ctypes.c_float
         _lib.orc_log.argtypes = [ctypes.c_float]
+        _lib.orc_dd_snr.restype = ctypes.c_float
     return _lib
 
 
@@ -49,6 +50,7 @@ def ref():
         if path is None:
             return None
         _ref = ctypes.CDLL(path)
+        _ref.ref_dd_snr.restype = ctypes.c_float
     return _ref
 
 
@@ -195,3 +197,12 @@ def bb_build(data, kbch, ts_gs=0):
     out = np.zeros(kbch, np.uint8)
     assert lib().orc_bb_build(_p(data, ctypes.c_uint8), len(data), kbch, ts_gs, _p(out, ctypes.c_uint8)) == 0
     return out
+
+
+def dd_snr(sym, pts, stride=1, qpsk=False):
+    """Decision-directed SNR (linear) of float32 (re, im) symbols against
+    points [2 * n_points] (ignored for QPSK)."""
+    sym = np.ascontiguousarray(sym, np.float32)
+    pts = np.ascontiguousarray(pts, np.float32)
+    return float(lib().orc_dd_snr(_p(sym, ctypes.c_float), sym.size // 2, _p(pts, ctypes.c_float),
+                                  pts.size // 2, stride, 1 if qpsk else 0))

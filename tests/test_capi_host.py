@@ -43,7 +43,11 @@ def test_no_device_is_a_loud_error(built_lib):
               lambda: cs.bch_check_cuda.for_code(E.FECFRAME_NORMAL, E.RATE_3_5),
               lambda: cs.batch([(E.MOD_QPSK, E.RATE_1_2, E.FECFRAME_SHORT)], 20, 8),
               lambda: cs.server([(E.MOD_QPSK, E.RATE_1_2, E.FECFRAME_SHORT)], 20, 64 << 20, 1, 8),
-              lambda: learned.nms_trainer(E.FECFRAME_SHORT, E.RATE_1_2, 5, 4)]
+              lambda: learned.nms_trainer(E.FECFRAME_SHORT, E.RATE_1_2, 5, 4),
+              lambda: cs.rx_fec_chain(E.FECFRAME_SHORT, E.RATE_1_2, E.MOD_QPSK, 20, 64, 2, 4),
+              lambda: cs.rx_fec_pool(E.FECFRAME_SHORT, [4, 12], 20, 64, 2, 4),
+              lambda: cs.gpu_decode_budget.make_default(),
+              lambda: cs.bb_extractor(E.FECFRAME_SHORT, E.RATE_1_2)]
     for make in makers:
         with pytest.raises(cs.CusatError) as e:
             make()

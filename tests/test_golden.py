@@ -69,3 +69,26 @@ def test_bb_scrambler_and_bbframes():
         assert plain[:10].tobytes().hex() == b["header"]
         out, lengths, _ = O.bb_extract(scr[None], kbch, [3], [1], kbch)
         assert lengths[0] == b["extracted"] == len(data) and (out == data).all()
+
+
+def _dd_symbols(seed, n=2000):
+    # same draw as tests/golden/make_golden.py:dd_symbols
+    if seed == 0:
+        a = np.float32(np.sqrt(0.5))
+        s = np.random.default_rng(7).integers(0, 2, 2 * n) * 2 - 1
+        return (s * a).astype(np.float32)
+    return np.random.default_rng(seed).uniform(-1.3, 1.3, 2 * n).astype(np.float32)
+
+
+def test_dd_snr_estimates(built_lib):
+    """The RX chain's decision-directed SNR (product and oracle) bit-exact
+    with the reference's qpsk_snr_dd / constellation_snr_dd."""
+    assert len(GOLD["dd_snr"]) >= 7
+    for c in GOLD["dd_snr"]:
+        sym = _dd_symbols(c["seed"])
+        want = np.uint32(c["value"]).view(np.float32)
+        got = cs.dd_snr(c["mod"], c["rate"], c["fs"], sym, stride=c["stride"])
+        pts = cs.modcod_info(c["mod"], c["rate"], c["fs"])["points"].view(np.float32)
+        orc = O.dd_snr(sym, pts, c["stride"], qpsk=c["mod"] == E.MOD_QPSK)
+        assert np.float32(got).view(np.uint32) == c["value"], (c, got, want)
+        assert np.float32(orc).view(np.uint32) == c["value"], (c, orc, want)

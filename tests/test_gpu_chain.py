@@ -1,0 +1,238 @@
+"""Frame-at-a-time receive chain and pool (rx_fec_chain / rx_fec_pool
+semantics) against a model of the reference's chain built from the oracle:
+the same micro-batches, the same decision-directed SNR updates every 32
+frames, the oracle's demap -> decode -> BCH -> BB stage per micro-batch.
+Output bytes, data-field sizes and frame/error counts must be identical."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cusat_gb300 as cs
+import oracle_lib as O
+from channel import awgn, es_normalised
+from cusat_gb300 import enums as E
+
+pytestmark = pytest.mark.gpu
+
+NORMAL, SHORT = E.FECFRAME_NORMAL, E.FECFRAME_SHORT
+
+
+def traffic(mod, rate, fs, n, esn0_db, seed):
+    """n XFECFRAMEs of GSE BBFRAMEs: mostly good frames, every 7th sent 4 dB
+    below esn0_db (LDPC failures), every 9th carrying a TS stream (no GSE
+    output), every 11th with a broken BBHEADER."""
+    rng = np.random.default_rng(seed)
+    ci = cs.code_info(fs, rate)
+    kbch = ci["k_bch"] // 8
+    bb = np.zeros((n, kbch), np.uint8)
+    for f in range(n):
+        size = [1, kbch - 10, int(rng.integers(1, kbch - 10))][f % 3]
+        bb[f] = O.bb_build(rng.integers(0, 256, size, dtype=np.uint8), kbch, ts_gs=3 if f % 9 == 4 else 0)
+    bb[5::11, 3] ^= 0x40
+    sym = es_normalised(cs.map_frames(mod, rate, fs, cs.encode_frames(fs, rate, bb)))
+    out = np.zeros_like(sym)
+    for f in range(n):
+        out[f], _ = awgn(sym[f], esn0_db - (4.0 if f % 7 == 2 else 0.0), rng)
+    return out
+
+
+class OracleChain:
+    """The reference's chain with an unlimited budget: frames accumulate into
+    micro-batches, every 32nd submitted frame re-estimates the SNR, a full
+    micro-batch is decoded with the chain's current noise variance and gain."""
+
+    def __init__(self, mod, rate, fs, micro_batch, T):
+        self.mod, self.rate, self.fs, self.mb, self.T = mod, rate, fs, micro_batch, T
+        self.mi = cs.modcod_info(mod, rate, fs)
+        self.kbch = cs.code_info(fs, rate)["k_bch"] // 8
+        self.noise_var, self.llr_gain = np.float32(1.0), np.float32(4.0)
+        self.skip, self.pending = 0, []
+        self.out, self.dfl, self.frames, self.errors = [], [], 0, 0
+
+    def start_from(self, chain, snr_db, skip=0):
+        """The chain's SNR after update_snr(snr_db) (a pilot estimate) and its
+        frame count since the last SNR update (warmup submits one frame)."""
+        chain.update_snr(snr_db)
+        self.noise_var, self.llr_gain = np.float32(chain.noise_var()), np.float32(chain.precision())
+        self.skip = skip
+
+    def submit(self, sym):
+        self.skip += 1
+        if self.skip >= 32:
+            self.skip = 0
+            lin = np.float32(O.dd_snr(sym, self.mi["points"].view(np.float32), 8, qpsk=self.mod == E.MOD_QPSK))
+            if lin > 1:
+                self.noise_var = np.float32(1.0) / lin
+                self.llr_gain = min(np.float32(4.0) / self.noise_var, np.float32(1000.0))
+        self.pending.append(sym)
+        if len(self.pending) == self.mb:
+            self.run()
+
+    def run(self):
+        if not self.pending:
+            return
+        noisy = np.stack(self.pending)
+        self.pending = []
+        mi = self.mi
+        g = cs.capped_llr_gain(self.mod, self.rate, self.fs, float(self.llr_gain))
+        llr = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"],
+                      mi["kind"], mi["points"], mi["col_offset"], float(self.noise_var), g)
+        hard, trials = O.ldpc_decode(self.fs, self.rate, llr, self.T)
+        _, valid = O.bch_check(self.fs, self.rate, hard)
+        out, lengths, _ = O.bb_extract(hard, self.kbch, trials, valid, len(noisy) * self.kbch)
+        ok = (trials >= 0) & (valid != 0)
+        self.frames += len(noisy)
+        self.errors += int((~ok).sum())
+        self.dfl += [int(v) for v, g in zip(lengths, ok) if g and v > 0]
+        self.out.append(out)
+
+    def output(self):
+        return np.concatenate(self.out) if self.out else np.zeros(0, np.uint8)
+
+
+def run_chain(chain, frames):
+    """Submits every frame, collecting output whenever it is reported, then
+    flushes; returns (bytes, data-field sizes)."""
+    out, dfl = [], []
+    for f in frames:
+        if chain.submit_xfecframe(f):
+            out.append(chain.get_gse_output())
+            dfl += chain.gse_dfl_sizes()
+    chain.flush()
+    out.append(chain.get_gse_output())
+    dfl += chain.gse_dfl_sizes()
+    return np.concatenate(out), dfl
+
+
+@pytest.mark.parametrize("name,fs,n,mb,streams", [("qpsk1/2", SHORT, 45, 4, 2), ("8psk3/5", SHORT, 40, 8, 3),
+                                                  ("8psk3/5", NORMAL, 36, 5, 4)])
+def test_chain_matches_oracle(cuda, name, fs, n, mb, streams):
+    _, mod, rate, _, _, thr = E.find_modcod(name)
+    frames = traffic(mod, rate, fs, n, thr + 0.8, seed=n + mb)
+    chain = cs.rx_fec_chain(fs, rate, mod, 50, 64, streams, mb)
+    chain.set_decode_budget(cs.gpu_decode_budget(0))
+    ref = OracleChain(mod, rate, fs, mb, 50)
+    ref.start_from(chain, thr + 0.8)
+    out, dfl = run_chain(chain, frames)
+    for f in frames:
+        ref.submit(f)
+    ref.run()
+    assert chain.frame_count() == ref.frames == n
+    assert chain.frame_error_count() == ref.errors and ref.errors >= n // 7
+    assert dfl == ref.dfl and len(dfl) > n // 2
+    assert out.size == ref.output().size and (out == ref.output()).all()
+    assert chain.noise_var() == float(ref.noise_var) != 1.0   # one SNR update happened
+    assert chain.gpu_inflight() == 0 and chain.pending_count() == 0 and chain.gpu_drop_count() == 0
+
+
+def test_budget_defers_launches_and_keeps_order(cuda):
+    """A budget of one micro-batch: launches wait for drains (or are forced
+    by flush), the output is still the oracle's, the budget returns to 0."""
+    _, mod, rate, _, _, thr = E.find_modcod("qpsk1/2")
+    frames = traffic(mod, rate, SHORT, 30, thr + 0.8, seed=5)
+    budget = cs.gpu_decode_budget(4)
+    chain = cs.rx_fec_chain(SHORT, rate, mod, 50, 64, 4, 4)
+    chain.set_decode_budget(budget)
+    chain.set_block_when_full(True)
+    ref = OracleChain(mod, rate, SHORT, 4, 50)
+    ref.start_from(chain, thr + 0.8)
+    out, dfl = run_chain(chain, frames)
+    for f in frames:
+        ref.submit(f)
+    ref.run()
+    assert (out == ref.output()).all() and dfl == ref.dfl
+    assert budget.in_flight == 0 and budget.cap == 4
+    assert chain.force_drain_count() > 0
+
+
+def test_launch_lock_wraps_every_launch(cuda):
+    _, mod, rate, _, _, thr = E.find_modcod("qpsk1/2")
+    frames = traffic(mod, rate, SHORT, 10, thr + 1.0, seed=6)
+    chain = cs.rx_fec_chain(SHORT, rate, mod, 50, 64, 2, 3)
+    calls = {"lock": 0, "unlock": 0}
+    CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p)
+    lock = CB(lambda _: calls.__setitem__("lock", calls["lock"] + 1))
+    unlock = CB(lambda _: calls.__setitem__("unlock", calls["unlock"] + 1))
+    assert cs._capi.lib().cusat_rx_chain_set_launch_lock(chain._h, ctypes.cast(lock, ctypes.c_void_p),
+                                                         ctypes.cast(unlock, ctypes.c_void_p), None) == 0
+    run_chain(chain, frames)
+    assert calls["lock"] == calls["unlock"] == 4        # ceil(10 / 3) micro-batches
+    assert chain.frame_count() == 10
+
+
+def test_drops_warmup_reset_and_snr(cuda):
+    _, mod, rate, _, _, thr = E.find_modcod("8psk3/5")
+    chain = cs.rx_fec_chain(SHORT, rate, mod, 50, 64, 2, 4)
+    chain.warmup()
+    assert chain.frame_count() == 0 and chain.gpu_drop_count() == 0 and chain.force_drain_count() == 0
+    xfec = chain.xfecframe_len
+    assert chain.submit_xfecframe(np.zeros(2 * (xfec - 1), np.float32)) is False   # wrong length: dropped
+    assert (chain.frame_count(), chain.frame_error_count(), chain.gpu_drop_count()) == (1, 1, 1)
+    chain.update_snr(10.0)
+    assert abs(chain.noise_var() - 0.1) < 1e-6 and abs(chain.precision() - 40.0) < 1e-3
+    assert chain.snr_db() == 10.0
+    chain.update_snr(-3.0)                                  # ignored, like the reference
+    assert chain.snr_db() == 10.0
+    frames = traffic(mod, rate, SHORT, 6, thr + 1.0, seed=7)
+    for f in frames:
+        chain.submit_xfecframe(f)
+    assert chain.pending_count() == 2
+    chain.reset()
+    assert (chain.frame_count(), chain.frame_error_count(), chain.pending_count(), chain.gpu_inflight()) == \
+        (0, 0, 0, 0)
+    assert chain.noise_var() == 1.0 and chain.precision() == 4.0
+
+
+def test_pool_output_in_submission_order(cuda):
+    """Two MODCODs in runs: each change flushes the previous chain, so the
+    pool's output blocks, concatenated, are the oracle's in submission order;
+    per-MODCOD counters follow."""
+    A, B = 4, 12                                        # qpsk1/2, 8psk3/5
+    pool = cs.rx_fec_pool(SHORT, [A, B], 50, 64, 2, 4)
+    pool.warmup_all()
+    models, frames = {}, {}
+    for idx in (A, B):
+        m = E.modcod_by_index(idx)
+        frames[idx] = list(traffic(m[1], m[2], SHORT, 22, m[5] + 0.8, seed=idx))
+        models[idx] = OracleChain(m[1], m[2], SHORT, 4, 50)
+        models[idx].start_from(pool.chain(idx), m[5] + 0.8, skip=1)
+    runs = [(A, 6), (B, 5), (A, 3), (B, 9), (A, 13), (B, 8)]
+    out, dfl, expect_out, expect_dfl = [], [], [], []
+    last = None
+    for idx, k in runs:
+        if last is not None and last != idx:
+            models[last].run()
+            expect_out.append(models[last].output())
+            expect_dfl += models[last].dfl
+            models[last].out, models[last].dfl = [], []
+        for _ in range(k):
+            f = frames[idx].pop(0)
+            models[idx].submit(f)
+            if pool.submit(f, idx):
+                while True:
+                    o = pool.get_gse_output()
+                    if o.size == 0:
+                        break
+                    out.append(o)
+                    dfl += pool.gse_dfl_sizes()
+        last = idx
+    pool.finish_all_pending()
+    while True:
+        o = pool.get_gse_output()
+        if o.size == 0:
+            break
+        out.append(o)
+        dfl += pool.gse_dfl_sizes()
+    models[last].run()
+    expect_out.append(models[last].output())
+    expect_dfl += models[last].dfl
+    got, want = np.concatenate(out), np.concatenate(expect_out)
+    assert got.size == want.size and (got == want).all() and dfl == expect_dfl
+    for idx in (A, B):
+        assert pool.modcod_counters(idx) == (models[idx].frames, models[idx].errors)
+    assert pool.modcod_counters(99) is None
+    assert pool.total_frame_count() == 44
+    assert pool.submit(np.zeros(2 * pool.chain(A).xfecframe_len, np.float32), 99) is False   # not enabled
+    pool.reset_all()
+    assert pool.total_frame_count() == 0

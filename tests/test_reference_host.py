@@ -101,3 +101,27 @@ def test_message_update_against_reference():
             d = np.zeros(1, np.int32)
             m = ref.ref_bnl_update(raw, old, ctypes.c_void_p(_p(d)))
             assert (m, int(d[0])) == O.bnl_update(raw, old)
+
+
+@pytest.mark.parametrize("mod,rate,fs", [(E.MOD_QPSK, E.RATE_1_2, 1), (E.MOD_8PSK, E.RATE_3_5, 0),
+                                         (E.MOD_16APSK, E.RATE_3_4, 0), (E.MOD_32APSK, E.RATE_3_4, 0),
+                                         (E.MOD_64APSK, E.RATE_4_5, 0)])
+def test_dd_snr_matches_reference(mod, rate, fs, built_lib):
+    """Decision-directed SNR: product and oracle bit-exact with the
+    reference's dd_snr.cc on noisy constellation points, every stride."""
+    mi = cs.modcod_info(mod, rate, fs)
+    pts = mi["points"]
+    rng = np.random.default_rng(mod * 100 + rate)
+    for sigma in (0.0, 0.05, 0.3, 1.0):
+        lab = rng.integers(0, len(pts), 3000)
+        z = pts[lab] + sigma * (rng.standard_normal(3000) + 1j * rng.standard_normal(3000))
+        sym = z.astype(np.complex64).view(np.float32)
+        for stride in (1, 8):
+            want = ref.ref_dd_snr(mod, rate, fs, ctypes.c_void_p(_p(sym)), 3000, stride,
+                                  1 if mod == E.MOD_QPSK else 0)
+            got = cs.dd_snr(mod, rate, fs, sym, stride=stride)
+            orc = O.dd_snr(sym, pts.view(np.float32), stride, qpsk=mod == E.MOD_QPSK)
+            assert np.float32(got) == np.float32(want) and np.float32(orc) == np.float32(want), (sigma, stride)
+    bad = np.full(20, np.nan, np.float32)
+    assert cs.dd_snr(mod, rate, fs, bad) == 0.0 == ref.ref_dd_snr(mod, rate, fs, ctypes.c_void_p(_p(bad)), 10, 1,
+                                                                 1 if mod == E.MOD_QPSK else 0)
