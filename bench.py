@@ -819,7 +819,9 @@ def codes_main(args, torch, cs, rank, local_rank, world):
                                "L2 for the short codes)", "codes": rows}}), flush=True)
 
 
-CHAIN_SETTINGS = [(4, 8), (16, 8), (64, 4)]   # (micro_batch, streams); (4, 8) is the reference's default
+# (micro_batch, streams, decode budget: -1 = one frame per SM, 0 = unlimited);
+# (4, 8, -1) is the reference's default
+CHAIN_SETTINGS = [(4, 8, -1), (16, 8, -1), (64, 4, -1), (64, 4, 0), (128, 4, 0), (256, 2, 0)]
 
 
 def chain_main(args, torch, cs, rank, local_rank, world):
@@ -836,8 +838,10 @@ def chain_main(args, torch, cs, rank, local_rank, world):
     rows = {}
     clocks = Clocks(local_rank)
     clocks.start()
-    for mb, streams in CHAIN_SETTINGS:
+    for mb, streams, cap in CHAIN_SETTINGS:
         chain = cs.rx_fec_chain(wl["fs"], wl["rate"], wl["mod"], wl["max_trials"], 64, streams, mb)
+        budget = cs.gpu_decode_budget(cap)
+        chain.set_decode_budget(budget)
         chain.set_block_when_full(True)
         chain.warmup()
         chain.update_snr(wl["esn0_db"])
@@ -847,16 +851,21 @@ def chain_main(args, torch, cs, rank, local_rank, world):
             k += 1
         chain.flush()
         n = args.steps * wl["frames"]
+        t_submit = 0.0
         t0 = time.perf_counter()
         for _ in range(n):
+            ta = time.perf_counter()
             chain.submit_xfecframe(frames[k % len(frames)])
+            t_submit += time.perf_counter() - ta
             k += 1
         chain.flush()
         dt = time.perf_counter() - t0
-        rows[f"micro_batch {mb}, {streams} streams"] = {
+        rows[f"micro_batch {mb}, {streams} streams, budget {budget.cap or 'unlimited'}"] = {
             "gbit_s": n * ci["k_ldpc"] / dt / 1e9, "ms_per_step": dt * 1e3 / args.steps,
-            "frames_per_s": n / dt, "force_drains": chain.force_drain_count(), "errors": chain.frame_error_count()}
+            "frames_per_s": n / dt, "host_us_per_submit": t_submit / n * 1e6,
+            "force_drains": chain.force_drain_count(), "errors": chain.frame_error_count()}
         chain.close()
+        budget.close()
     clk = clocks.stop()
     if rank != 0:
         return
@@ -867,7 +876,7 @@ def chain_main(args, torch, cs, rank, local_rank, world):
         "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded 8PSK 3/5 normal frames at 6 dB, host "
                                                        "memory, random payloads)",
         "config": {"workload": "rx_fec_chain: frames submitted one at a time from host memory, 256 per step, "
-                               "default decode budget, max 50 iterations", "settings": rows,
+                               "max 50 iterations", "settings": rows,
                    "e2e_note": "host symbols in, per-frame verdicts and GSE data fields out (pinned)"},
         "clocks": clk}), flush=True)
 

@@ -39,7 +39,6 @@ struct KernelClass {
     cusat::DecodeArgs proto{};
     std::vector<int> modcods;  // modcod indices, position = code index in the class
     cusat::DevCode* d_codes = nullptr;
-    cusat::DevDemap* d_demaps = nullptr;
     cusat::FrameDesc* d_frames = nullptr;
     uint4* msg = nullptr;
     unsigned int* queue = nullptr;
@@ -59,9 +58,14 @@ struct cusat_batch {
     // staging (pinned) and device descriptors
     cusat::FrameDesc* h_frames = nullptr;   // [max_frames], grouped by class
     cusat::BchFrame* h_bch = nullptr;       // [max_frames]
+    cusat::DemapFrame* h_demap = nullptr;   // [max_frames]
     cusat::FrameDesc* d_frames = nullptr;
     cusat::BchFrame* d_bch = nullptr;
+    cusat::DemapFrame* d_demap = nullptr;
     cusat::BchDev* d_bch_codes = nullptr;
+    cusat::DevDemap* d_demap_params = nullptr;  // [modcods]
+    int16_t* llr = nullptr;                     // [max_frames][max_n] demapped LLRs
+    int max_n = 0, max_len = 0;                 // largest code length, largest interleaved length
     std::vector<int> class_count, class_off;
     cudaEvent_t fork = nullptr;
     // captured sequence: its own device descriptors (written once at capture),
@@ -69,6 +73,7 @@ struct cusat_batch {
     cudaGraphExec_t graph = nullptr;
     cusat::FrameDesc* g_frames = nullptr;
     cusat::BchFrame* g_bch = nullptr;
+    cusat::DemapFrame* g_demap = nullptr;
     int graph_frames = 0;
 };
 
@@ -82,7 +87,6 @@ void release(cusat_batch* b)
         cudaGraphExecDestroy(b->graph);
     for (auto& c : b->classes) {
         if (c.d_codes) cudaFree(c.d_codes);
-        if (c.d_demaps) cudaFree(c.d_demaps);
         if (c.msg) cudaFree(c.msg);
         if (c.queue) cudaFree(c.queue);
         if (c.stream) cudaStreamDestroy(c.stream);
@@ -96,11 +100,16 @@ void release(cusat_batch* b)
     }
     if (b->h_frames) cudaFreeHost(b->h_frames);
     if (b->h_bch) cudaFreeHost(b->h_bch);
+    if (b->h_demap) cudaFreeHost(b->h_demap);
     if (b->d_frames) cudaFree(b->d_frames);
     if (b->d_bch) cudaFree(b->d_bch);
+    if (b->d_demap) cudaFree(b->d_demap);
     if (b->d_bch_codes) cudaFree(b->d_bch_codes);
+    if (b->d_demap_params) cudaFree(b->d_demap_params);
+    if (b->llr) cudaFree(b->llr);
     if (b->g_frames) cudaFree(b->g_frames);
     if (b->g_bch) cudaFree(b->g_bch);
+    if (b->g_demap) cudaFree(b->g_demap);
     if (b->fork) cudaEventDestroy(b->fork);
     delete b;
 }
@@ -133,12 +142,18 @@ int stage(cusat_batch* b, const cusat_frame* frames, int n)
     for (int k = 0; k < n; k++) {
         const cusat_frame& fr = frames[idx[k]];
         const ModcodObj& m = *b->modcods[fr.modcod];
+        int16_t* llr = b->llr + (size_t)k * b->max_n;
+        cusat::DemapFrame& q = b->h_demap[k];
+        q.modcod = fr.modcod;
+        q.noise_var = fr.noise_var;
+        q.llr_gain = cusat::capped_llr_gain(m.dm.m, fr.llr_gain);
+        q.pad = 0;
+        q.sym = reinterpret_cast<const float2*>(fr.sym);
+        q.out = llr;
         cusat::FrameDesc& d = b->h_frames[k];
         d.code = m.code_in_class;
-        d.noise_var = fr.noise_var;
-        d.llr_gain = cusat::capped_llr_gain(m.dm.m, fr.llr_gain);
-        d.pad = 0;
-        d.in = fr.sym;
+        d.pad[0] = d.pad[1] = d.pad[2] = 0;
+        d.llr = llr;
         d.hard = fr.hard;
         d.trials = fr.trials;
         cusat::BchFrame& c = b->h_bch[k];
@@ -151,15 +166,24 @@ int stage(cusat_batch* b, const cusat_frame* frames, int n)
 }
 
 // Launch sequence for n staged frames whose descriptors are (or, with
-// `copy`, are first copied from the pinned staging arrays) at d_frames/d_bch.
-int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, cusat::BchFrame* d_bch, bool copy)
+// `copy`, are first copied from the pinned staging arrays) at
+// d_frames/d_bch/d_demap: the demap of every frame over the whole grid,
+// then one decoder launch per kernel class on its own stream, then the BCH
+// check of every frame.
+int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, cusat::BchFrame* d_bch,
+            cusat::DemapFrame* d_demap, bool copy)
 {
     if (copy) {
         CU(cudaMemcpyAsync(d_frames, b->h_frames, (size_t)n * sizeof(cusat::FrameDesc), cudaMemcpyHostToDevice, s),
            "cudaMemcpyAsync(frames)");
         CU(cudaMemcpyAsync(d_bch, b->h_bch, (size_t)n * sizeof(cusat::BchFrame), cudaMemcpyHostToDevice, s),
            "cudaMemcpyAsync(bch frames)");
+        CU(cudaMemcpyAsync(d_demap, b->h_demap, (size_t)n * sizeof(cusat::DemapFrame), cudaMemcpyHostToDevice, s),
+           "cudaMemcpyAsync(demap frames)");
     }
+    const int dr = cusat::launch_demap_mixed(b->d_demap_params, d_demap, n, b->max_len, s);
+    if (dr)
+        return cuda_fail((cudaError_t)dr, "demap launch");
     CU(cudaEventRecord(b->fork, s), "cudaEventRecord");
     for (int k : b->order) {
         KernelClass& c = b->classes[k];
@@ -243,10 +267,9 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
     // message scratch for every resident CTA, stream
     for (size_t k = 0; k < b->classes.size() && rc == CUSAT_OK; k++) {
         KernelClass& c = b->classes[k];
-        cusat::SmemDims dims{0, 0, 0, 0, c.cmax, 0, c.lanes};
+        cusat::SmemDims dims{0, 0, 0, 0, c.cmax, c.lanes};
         size_t msg_cta = 0;
         std::vector<cusat::DevCode> codes;
-        std::vector<cusat::DevDemap> demaps;
         for (int mi : c.modcods) {
             const ModcodObj& m = *b->modcods[mi];
             const cusat::DevCode& dc = m.dp.code;
@@ -254,12 +277,10 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
             dims.q = std::max(dims.q, dc.q);
             dims.n_steps = std::max(dims.n_steps, dc.n_steps);
             dims.n_items = std::max(dims.n_items, dc.n_items);
-            dims.n_points = std::max(dims.n_points, m.dm.m.kind == 2 ? m.dm.m.n_points : 0);
             msg_cta = std::max(msg_cta, (size_t)dc.R * dc.msg_row);
             codes.push_back(dc);
-            demaps.push_back(m.dm.d);
         }
-        c.fn = cusat::select_decoder_kernel(c.cmax, c.lanes, true);
+        c.fn = cusat::select_decoder_kernel(c.cmax, c.lanes);
         c.threads = cusat::decoder_threads(c.lanes);
         memset(&c.proto, 0, sizeof(c.proto));
         c.proto.max_trials = max_trials;
@@ -277,11 +298,6 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
         if (e == cudaSuccess)
             e = cudaMemcpy(c.d_codes, codes.data(), codes.size() * sizeof(cusat::DevCode), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
-            e = cudaMalloc(&c.d_demaps, demaps.size() * sizeof(cusat::DevDemap));
-        if (e == cudaSuccess)
-            e = cudaMemcpy(c.d_demaps, demaps.data(), demaps.size() * sizeof(cusat::DevDemap),
-                           cudaMemcpyHostToDevice);
-        if (e == cudaSuccess)
             e = cudaMalloc(&c.msg, (size_t)c.grid_max * msg_cta);
         if (e == cudaSuccess)
             e = cudaMalloc(&c.queue, 256);
@@ -294,7 +310,6 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
             break;
         }
         c.proto.codes = c.d_codes;
-        c.proto.demaps = c.d_demaps;
         c.proto.msg = c.msg;
         c.proto.msg_stride = (int)(msg_cta / 16);
         c.proto.queue = c.queue;
@@ -302,9 +317,26 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
     }
     if (rc == CUSAT_OK) {
         std::vector<cusat::BchDev> bch;
-        for (auto& m : b->modcods)
+        std::vector<cusat::DevDemap> demaps;
+        for (auto& m : b->modcods) {
             bch.push_back(m->bch.d);
+            demaps.push_back(m->dm.d);
+            b->max_n = std::max(b->max_n, m->plan->N);
+            b->max_len = std::max(b->max_len, m->dm.m.interleaved_len);
+        }
+        b->max_n = (b->max_n + 7) & ~7;  // 16-byte aligned LLR rows
         cudaError_t e = cudaMallocHost(&b->h_frames, (size_t)max_frames * sizeof(cusat::FrameDesc));
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&b->h_demap, (size_t)max_frames * sizeof(cusat::DemapFrame));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&b->d_demap, (size_t)max_frames * sizeof(cusat::DemapFrame));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&b->d_demap_params, demaps.size() * sizeof(cusat::DevDemap));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_demap_params, demaps.data(), demaps.size() * sizeof(cusat::DevDemap),
+                           cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&b->llr, (size_t)max_frames * b->max_n * sizeof(int16_t));
         if (e == cudaSuccess)
             e = cudaMallocHost(&b->h_bch, (size_t)max_frames * sizeof(cusat::BchFrame));
         if (e == cudaSuccess)
@@ -372,7 +404,7 @@ int batch_launch_ready(cusat_batch* b, const cusat_frame* frames, int n, cudaStr
     const int rc = stage(b, frames, n);
     if (rc)
         return rc;
-    return enqueue(b, n, stream, b->d_frames, b->d_bch, true);
+    return enqueue(b, n, stream, b->d_frames, b->d_bch, b->d_demap, true);
 }
 
 }  // namespace cusat_internal
@@ -388,7 +420,7 @@ int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* s
     int rc = stage(b, frames, n);
     if (rc)
         return rc;
-    return enqueue(b, n, (cudaStream_t)stream, b->d_frames, b->d_bch, true);
+    return enqueue(b, n, (cudaStream_t)stream, b->d_frames, b->d_bch, b->d_demap, true);
 }
 
 int cusat_batch_capture(cusat_batch* b, const cusat_frame* frames, int n, void* stream)
@@ -409,13 +441,16 @@ int cusat_batch_capture(cusat_batch* b, const cusat_frame* frames, int n, void* 
     if (!b->g_frames) {
         CU(cudaMalloc(&b->g_frames, (size_t)b->max_frames * sizeof(cusat::FrameDesc)), "cudaMalloc(graph frames)");
         CU(cudaMalloc(&b->g_bch, (size_t)b->max_frames * sizeof(cusat::BchFrame)), "cudaMalloc(graph frames)");
+        CU(cudaMalloc(&b->g_demap, (size_t)b->max_frames * sizeof(cusat::DemapFrame)), "cudaMalloc(graph frames)");
     }
     CU(cudaMemcpy(b->g_frames, b->h_frames, (size_t)n * sizeof(cusat::FrameDesc), cudaMemcpyHostToDevice),
        "cudaMemcpy(graph frames)");
     CU(cudaMemcpy(b->g_bch, b->h_bch, (size_t)n * sizeof(cusat::BchFrame), cudaMemcpyHostToDevice),
        "cudaMemcpy(graph frames)");
+    CU(cudaMemcpy(b->g_demap, b->h_demap, (size_t)n * sizeof(cusat::DemapFrame), cudaMemcpyHostToDevice),
+       "cudaMemcpy(graph frames)");
     CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-    rc = enqueue(b, n, s, b->g_frames, b->g_bch, false);
+    rc = enqueue(b, n, s, b->g_frames, b->g_bch, b->g_demap, false);
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(s, &g);
     if (rc)
@@ -479,7 +514,7 @@ int cusat_batch_tune(cusat_batch* b, const cusat_frame* frames, int n, int reps,
         float sum = 0;
         for (int r = 0; r <= reps; r++) {
             CU(cudaEventRecord(e0, s), "cudaEventRecord");
-            rc = enqueue(b, n, s, b->d_frames, b->d_bch, true);
+            rc = enqueue(b, n, s, b->d_frames, b->d_bch, b->d_demap, true);
             if (rc)
                 break;
             CU(cudaEventRecord(e1, s), "cudaEventRecord");

@@ -49,7 +49,7 @@ struct Engine {
         return CUSAT_OK;
     }
 
-    int init(const cusat::CodePlan* p, int trials, int batch, bool fused, int n_points)
+    int init(const cusat::CodePlan* p, int trials, int batch)
     {
         plan = p;
         max_trials = trials;
@@ -60,14 +60,14 @@ struct Engine {
         rc = upload_plan(*p, &dp);
         if (rc)
             return rc;
-        fn = cusat::select_decoder_kernel(p->cmax, p->lanes, fused);
+        fn = cusat::select_decoder_kernel(p->cmax, p->lanes);
         if (!fn)
             return fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel for this check degree");
         threads = cusat::decoder_threads(p->lanes);
         memset(&proto, 0, sizeof(proto));
         proto.code = dp.code;
         proto.max_trials = max_trials;
-        cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, n_points, p->lanes));
+        cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, p->lanes));
         int optin = 0, sms = 0;
         CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
@@ -142,6 +142,7 @@ struct cusat_rx_fec {
     Engine eng;
     DevDemapObj dm;
     DevBch bch;
+    int16_t* llr = nullptr;  // [max_batch][N] demapped LLRs
 };
 
 extern "C" {
@@ -163,7 +164,7 @@ int cusat_ldpc_decoder_create(int framesize, int rate, int max_trials, int max_b
     if (!p)
         return fail(CUSAT_ERR_UNSUPPORTED, err);
     cusat_ldpc_decoder* d = new cusat_ldpc_decoder();
-    int rc = d->eng.init(p, max_trials, max_batch, false, 0);
+    int rc = d->eng.init(p, max_trials, max_batch);
     if (rc == CUSAT_OK) {
         cudaError_t e = cudaMalloc(&d->soft_dev, (size_t)max_batch * p->N * 2);
         if (e == cudaSuccess)
@@ -479,11 +480,13 @@ int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials,
     cusat_rx_fec* r = new cusat_rx_fec();
     int rc = r->dm.init(modulation, rate, framesize);
     if (rc == CUSAT_OK)
-        rc = r->eng.init(p, max_trials, max_batch, true, r->dm.m.kind == 2 ? r->dm.m.n_points : 0);
+        rc = r->eng.init(p, max_trials, max_batch);
     if (rc == CUSAT_OK)
         rc = r->bch.init(p->gen, p->p, (unsigned)(p->n_bch / 8));
     if (rc == CUSAT_OK) {
-        r->eng.proto.dm = r->dm.d;
+        const cudaError_t e = cudaMalloc(&r->llr, (size_t)max_batch * p->N * sizeof(int16_t));
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "cudaMalloc(LLRs)");
     }
     if (rc != CUSAT_OK) {
         cusat_rx_fec_destroy(r);
@@ -500,6 +503,8 @@ void cusat_rx_fec_destroy(cusat_rx_fec* r)
     r->eng.release();
     r->dm.release();
     r->bch.release();
+    if (r->llr)
+        cudaFree(r->llr);
     delete r;
 }
 
@@ -538,10 +543,15 @@ int cusat_rx_fec_launch(cusat_rx_fec* r, const float* sym_dev, int batch, float 
         return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
     if (r->dm.m.interleaved_len != r->dm.m.xfec)
         return fail(CUSAT_ERR_UNSUPPORTED, "padded XFECFRAME");
+    // demap + deinterleave over the whole grid into HBM, then decode: the
+    // decoder holds one frame per SM, and a demap inside it would run at one
+    // CTA's memory parallelism
+    const int e = cusat::launch_demap(r->dm.d, sym_dev, batch, noise_var, cusat::capped_llr_gain(r->dm.m, llr_gain),
+                                      r->llr, (cudaStream_t)stream);
+    if (e)
+        return cuda_fail((cudaError_t)e, "demap launch");
     cusat::DecodeArgs a = r->eng.proto;
-    a.sym = sym_dev;
-    a.noise_var = noise_var;
-    a.llr_gain = cusat::capped_llr_gain(r->dm.m, llr_gain);
+    a.llr = r->llr;
     a.hard = hard_out;
     a.trials = trials_out;
     int rc = r->eng.launch(a, batch, (cudaStream_t)stream);

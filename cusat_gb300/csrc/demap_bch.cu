@@ -34,9 +34,49 @@ __global__ void __launch_bounds__(256) demap_kernel(DevDemap d, const float2* __
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream)
 {
-    dim3 grid((d.interleaved_len + 255) / 256, batch);
-    demap_kernel<<<grid, 256, 0, stream>>>(d, reinterpret_cast<const float2*>(sym), out, noise_var,
-                                           llr_gain);
+    for (int f0 = 0; f0 < batch; f0 += 65535) {
+        dim3 grid((d.interleaved_len + 255) / 256, batch - f0 < 65535 ? batch - f0 : 65535);
+        demap_kernel<<<grid, 256, 0, stream>>>(d, reinterpret_cast<const float2*>(sym) + (size_t)f0 * d.xfec,
+                                               out + (size_t)f0 * d.fec_len, noise_var, llr_gain);
+    }
+    return (int)cudaGetLastError();
+}
+
+// Mixed batch: grid.y = frame, each frame's MODCOD parameters (and points)
+// staged in shared memory, blocks stride over the frame's symbols.
+__global__ void __launch_bounds__(256) demap_mixed_kernel(const DevDemap* __restrict__ demaps,
+                                                         const DemapFrame* __restrict__ frames)
+{
+    __shared__ float2 pts[256];
+    __shared__ DevDemap d;
+    const DemapFrame fr = frames[blockIdx.y];
+    if (threadIdx.x == 0)
+        d = demaps[fr.modcod];
+    __syncthreads();
+    if (d.kind == 2)
+        for (int k = threadIdx.x; k < d.n_points; k += blockDim.x)
+            pts[k] = d.points[k];
+    __syncthreads();
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < d.interleaved_len; j += gridDim.x * blockDim.x) {
+        const float2 s = __ldcs(fr.sym + j);
+        int pos[8];
+        int16_t l[8];
+        const int nb = demap_symbol(d, pts, s.x, s.y, j, fr.noise_var, fr.llr_gain, pos, l);
+#pragma unroll
+        for (int b = 0; b < 8; b++)
+            if (b < nb && pos[b] < d.fec_len)
+                fr.out[pos[b]] = l[b];
+    }
+}
+
+int launch_demap_mixed(const DevDemap* demaps, const DemapFrame* frames, int n, int max_len, cudaStream_t stream)
+{
+    // 4 symbols per thread for the longest frame: about 32 blocks per
+    // normal-frame QPSK frame, 128 threads' worth of work per block
+    for (int f0 = 0; f0 < n; f0 += 65535) {
+        dim3 grid((max_len + 1023) / 1024, n - f0 < 65535 ? n - f0 : 65535);
+        demap_mixed_kernel<<<grid, 256, 0, stream>>>(demaps, frames + f0);
+    }
     return (int)cudaGetLastError();
 }
 

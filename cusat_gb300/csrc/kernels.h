@@ -36,19 +36,30 @@ struct DecoderKernelInfo {
 
 // Largest code dimensions a decoder launch must hold in shared memory.
 struct SmemDims {
-    int N, q, n_steps, n_items, cmax, n_points, lanes;
+    int N, q, n_steps, n_items, cmax, lanes;
 };
 
-// The kernel instantiation for (cmax, lanes, fused), or nullptr.
-const void* select_decoder_kernel(int cmax, int lanes, bool fused);
+// The kernel instantiation for (cmax, lanes), or nullptr.
+const void* select_decoder_kernel(int cmax, int lanes);
 // Fills the shared-memory carve-up of a for codes up to d.
 void decoder_smem_layout(DecodeArgs* a, const SmemDims& d);
-SmemDims smem_dims_of(const DevCode& c, int n_points, int lanes);
+SmemDims smem_dims_of(const DevCode& c, int lanes);
 int decoder_threads(int lanes);
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
 
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream);
+// One frame of a mixed demap launch (device memory).
+struct DemapFrame {
+    int modcod;              // index into the launch's DevDemap array
+    float noise_var, llr_gain;
+    int pad;
+    const float2* sym;       // [xfec] symbols
+    int16_t* out;            // [fec_len] LLRs
+};
+// Demaps n frames of any of the given MODCODs; max_len = the largest
+// interleaved length among them.
+int launch_demap_mixed(const DevDemap* demaps, const DemapFrame* frames, int n, int max_len, cudaStream_t stream);
 // Sets the message returned by cusat_last_error() on this thread.
 void set_last_error(const std::string& msg);
 

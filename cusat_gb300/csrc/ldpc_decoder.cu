@@ -7,28 +7,24 @@ namespace cusat {
 namespace {
 
 template <int CMAX>
-const void* pick(int lanes, bool fused)
+const void* pick(int lanes)
 {
-    if (lanes == 2)
-        return fused ? (const void*)ldpc_layered_kernel<CMAX, 2, true>
-                     : (const void*)ldpc_layered_kernel<CMAX, 2, false>;
-    return fused ? (const void*)ldpc_layered_kernel<CMAX, 1, true>
-                 : (const void*)ldpc_layered_kernel<CMAX, 1, false>;
+    return lanes == 2 ? (const void*)ldpc_layered_kernel<CMAX, 2> : (const void*)ldpc_layered_kernel<CMAX, 1>;
 }
 
 int align16(int x) { return (x + 15) & ~15; }
 
 }  // namespace
 
-const void* select_decoder_kernel(int cmax, int lanes, bool fused)
+const void* select_decoder_kernel(int cmax, int lanes)
 {
     switch (cmax) {
-    case 3: return pick<3>(lanes, fused);
-    case 5: return pick<5>(lanes, fused);
-    case 9: return pick<9>(lanes, fused);
-    case 14: return pick<14>(lanes, fused);
-    case 20: return pick<20>(lanes, fused);
-    case 28: return pick<28>(lanes, fused);
+    case 3: return pick<3>(lanes);
+    case 5: return pick<5>(lanes);
+    case 9: return pick<9>(lanes);
+    case 14: return pick<14>(lanes);
+    case 20: return pick<20>(lanes);
+    case 28: return pick<28>(lanes);
     default: return nullptr;
     }
 }
@@ -50,8 +46,7 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     take(&a->sm_conf, d.n_steps);
     take(&a->sm_item_off, (d.n_steps + 1) * 2);
     take(&a->sm_items, d.n_items * 8);
-    take(&a->sm_pts, d.n_points * 8);
-    take(&a->sm_code, (int)(sizeof(DevCode) + 8 + sizeof(DevDemap)));
+    take(&a->sm_code, (int)sizeof(DevCode));
     take(&a->sm_misc, 16);
     // message rows staged for the next step: two sets x threads x row words
     const int rw = (d.cmax + 2 + 15) / 16;
@@ -59,9 +54,9 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     a->sm_total = off;
 }
 
-SmemDims smem_dims_of(const DevCode& c, int n_points, int lanes)
+SmemDims smem_dims_of(const DevCode& c, int lanes)
 {
-    return SmemDims{c.N, c.q, c.n_steps, c.n_items, c.cmax, n_points, lanes};
+    return SmemDims{c.N, c.q, c.n_steps, c.n_items, c.cmax, lanes};
 }
 
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream)

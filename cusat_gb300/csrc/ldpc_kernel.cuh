@@ -47,23 +47,18 @@ namespace cusat {
 
 // One frame of a mixed batch (device memory).
 struct FrameDesc {
-    int code;                // index into DecodeArgs::codes / demaps
-    float noise_var, llr_gain;
-    int pad;
-    const void* in;          // int16 LLRs [N] or complex symbols [xfec]
+    int code;                // index into DecodeArgs::codes
+    int pad[3];
+    const int16_t* llr;      // [N] channel LLRs
     uint8_t* hard;           // [K/8]
     int32_t* trials;         // [1]
 };
 
 struct DecodeArgs {
     DevCode code;            // single-code launch (codes == nullptr)
-    DevDemap dm;             // fused demap of the single-code launch
     const DevCode* codes;    // mixed batch: per-code tables, frames[f].code indexes them
-    const DevDemap* demaps;
     const FrameDesc* frames;
-    const int16_t* llr;      // single code: [n_frames][N] int16 LLRs (unfused)
-    const float* sym;        // single code: [n_frames][xfec][2] symbols (fused)
-    float noise_var, llr_gain;
+    const int16_t* llr;      // single code: [n_frames][N] int16 LLRs
     int n_frames, max_trials;
     uint8_t* hard;           // single code: [n_frames][K/8]
     int32_t* trials;         // single code: [n_frames]
@@ -71,16 +66,15 @@ struct DecodeArgs {
     int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
     unsigned int* queue;     // frame counter, zero at launch
     // shared-memory carve-up (bytes)
-    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_pts, sm_code, sm_misc, sm_msgbuf,
+    int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_code, sm_misc, sm_msgbuf,
         sm_total;
 };
 
 // Where one frame comes from and goes to.
 struct Job {
-    const void* in;
+    const int16_t* llr;
     uint8_t* hard;
     int32_t* trials;
-    float noise_var, llr_gain;
 };
 
 // Shared-memory views of the code tables.
@@ -288,17 +282,22 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
         m1 = min(max(r1 - 1, 0), 127);
         m2 = min(max(r2 - 1, 0), 127);
     }
-    // each message carries the sign product of the other edges
+    // each message carries the sign product of the other edges.  Per edge,
+    // in multiply-add form (FMA pipe; the ALU pipe is the busier one):
+    // s = sign of the extrinsic (+1 / -1), t = 0 iff |d| is the minimum,
+    // message = s * (t ? p1 : p2)
     const int sg = sx >> 31;
     const int p1 = madd(sg, neg, m1 ^ sg), p2 = madd(sg, neg, m2 ^ sg);
+    const int dp = p1 - p2, nr1 = -r1, two = one + one;
     uint32_t wv[RW * 4];
 #pragma unroll
     for (int k = 0; k < RW * 4; k++)
         wv[k] = 0;
 #pragma unroll
     for (int e = 0; e < NE; e++) {
-        const int ds = d[e] >> 31;
-        const int mg = madd(ds, neg, ((abs(d[e]) == r1) ? p2 : p1) ^ ds);
+        const int s = madd(d[e] >> 31, two, one);
+        const int t = min(madd(d[e], s, nr1), one);
+        const int mg = madd(madd(t, dp, p2), s, 0);
         wv[e >> 2] = __byte_perm(wv[e >> 2], (uint32_t)mg,
                                  (e & 3) == 0 ? 0x3214 : (e & 3) == 1 ? 0x3240 : (e & 3) == 2 ? 0x3410 : 0x4210);
         if (e < 2) {
@@ -498,52 +497,20 @@ __device__ __forceinline__ int load_llr(const DevCode& c, int16_t* app, const in
     return over;
 }
 
-// Fused demap + deinterleave of frame f's symbols straight into the APP.
-__device__ __forceinline__ int demap_into(const DevCode& c, const DevDemap& d, int16_t* app, const float2* pts,
-                                          const float2* src, float noise_var, float llr_gain)
-{
-    const int K = c.K, q = c.q, lim = c.fast_lim, N = c.N;
-    int over = 0;
-    for (int jj = threadIdx.x; jj < d.interleaved_len; jj += blockDim.x) {
-        const float2 s = __ldcs(src + jj);
-        int pos[8];
-        int16_t l[8];
-        const int nb = demap_symbol(d, pts, s.x, s.y, jj, noise_var, llr_gain, pos, l);
-#pragma unroll
-        for (int b = 0; b < 8; b++) {
-            if (b < nb && pos[b] < N) {
-                const int x = max((int)l[b], -32767);
-                over |= abs(x) > lim;
-                const int p = pos[b];
-                if (p < K)
-                    app[p] = (int16_t)x;
-                else
-                    app[K + ((p - K) % q) * kM + (p - K) / q] = (int16_t)x;
-            }
-        }
-    }
-    return over;
-}
-
-// Copies one code's tables (and demap points) into shared memory; the slot
-// descriptors are rebased onto this kernel's stage and dummy regions and
-// packed to 8 bytes: x = bit base, y = r | store offset << 9.
-template <int CMAX, bool FUSED>
-__device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCode& gc, const DevDemap& gd)
+// Copies one code's tables into shared memory; the slot descriptors are
+// rebased onto this kernel's stage and dummy regions.
+template <int CMAX>
+__device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCode& gc)
 {
     DevCode* s_code = reinterpret_cast<DevCode*>(smem + a.sm_code);
-    DevDemap* s_dm = reinterpret_cast<DevDemap*>(smem + a.sm_code + sizeof(DevCode) + 8);
     uint4* s_tab = reinterpret_cast<uint4*>(smem + a.sm_tab);
     uint8_t* s_cnt = smem + a.sm_cnt;
     int16_t* s_sched = reinterpret_cast<int16_t*>(smem + a.sm_sched);
     uint8_t* s_conf = smem + a.sm_conf;
     uint16_t* s_item_off = reinterpret_cast<uint16_t*>(smem + a.sm_item_off);
     uint2* s_items = reinterpret_cast<uint2*>(smem + a.sm_items);
-    float2* pts = reinterpret_cast<float2*>(smem + a.sm_pts);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0)
         *s_code = gc;
-        *s_dm = gd;
-    }
     for (int k = threadIdx.x; k < gc.q * CMAX; k += blockDim.x) {
         uint4 w = gc.tab[k];
         if (w.w == kSlotStaged)
@@ -566,12 +533,9 @@ __device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCod
         s_item_off[k] = gc.item_off[k];
     for (int k = threadIdx.x; k < gc.n_items; k += blockDim.x)
         s_items[k] = gc.items[k];
-    if (FUSED && gd.kind == 2)
-        for (int k = threadIdx.x; k < gd.n_points; k += blockDim.x)
-            pts[k] = gd.points[k];
 }
 
-template <int CMAX, int LANES, bool FUSED>
+template <int CMAX, int LANES>
 __global__ void __launch_bounds__(LANES * lane_threads(LANES), LANES == 2 ? 1 : 2) ldpc_layered_kernel(DecodeArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -579,8 +543,6 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), LANES == 2 ? 1 : 
     int16_t* dummy = reinterpret_cast<int16_t*>(smem + a.sm_dummy);
     const int16_t* stage = reinterpret_cast<const int16_t*>(smem + a.sm_stage);
     const DevCode& c = *reinterpret_cast<const DevCode*>(smem + a.sm_code);
-    const DevDemap& dm = *reinterpret_cast<const DevDemap*>(smem + a.sm_code + sizeof(DevCode) + 8);
-    const float2* pts = reinterpret_cast<const float2*>(smem + a.sm_pts);
     int* s_misc = reinterpret_cast<int*>(smem + a.sm_misc);
     const SmemCode t = {reinterpret_cast<const uint4*>(smem + a.sm_tab), smem + a.sm_cnt,
                         reinterpret_cast<const int16_t*>(smem + a.sm_sched), smem + a.sm_conf,
@@ -603,26 +565,19 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), LANES == 2 ? 1 : 
         if (a.frames) {
             const FrameDesc fd = a.frames[f];
             code_id = fd.code;
-            job = {fd.in, fd.hard, fd.trials, fd.noise_var, fd.llr_gain};
+            job = {fd.llr, fd.hard, fd.trials};
         }
         if (code_id != loaded) {
-            if (a.codes)
-                load_code<CMAX, FUSED>(a, smem, a.codes[code_id], FUSED ? a.demaps[code_id] : a.dm);
-            else
-                load_code<CMAX, FUSED>(a, smem, a.code, a.dm);
+            load_code<CMAX>(a, smem, a.codes ? a.codes[code_id] : a.code);
             loaded = code_id;
             __syncthreads();
         }
         if (!a.frames) {
-            job.in = FUSED ? (const void*)(a.sym + (size_t)f * 2 * dm.xfec) : (const void*)(a.llr + (size_t)f * c.N);
+            job.llr = a.llr + (size_t)f * c.N;
             job.hard = a.hard + (size_t)f * (c.K / 8);
             job.trials = a.trials + f;
-            job.noise_var = a.noise_var;
-            job.llr_gain = a.llr_gain;
         }
-        const int over = FUSED ? demap_into(c, dm, app, pts, reinterpret_cast<const float2*>(job.in), job.noise_var,
-                                            job.llr_gain)
-                               : load_llr(c, app, reinterpret_cast<const int16_t*>(job.in));
+        const int over = load_llr(c, app, job.llr);
         if (__syncthreads_or(over))
             decode_frame<CMAX, LANES, true>(a, c, smem, stage, t, job);
         else

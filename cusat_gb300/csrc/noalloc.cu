@@ -176,10 +176,10 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     a.msg = (uint4*)st.msg;
     a.msg_stride = p->R * p->msg_row / 16;
     a.queue = st.queue;
-    cusat::decoder_smem_layout(&a, cusat::smem_dims_of(a.code, 0, p->lanes));
+    cusat::decoder_smem_layout(&a, cusat::smem_dims_of(a.code, p->lanes));
     if (a.sm_total > st.optin)
         return fail(CUSAT_ERR_UNSUPPORTED, "frame state does not fit in shared memory");
-    const void* fn = cusat::select_decoder_kernel(p->cmax, p->lanes, false);
+    const void* fn = cusat::select_decoder_kernel(p->cmax, p->lanes);
     if (!fn)
         return fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel for this check degree");
     // the cap is shared by every object launching this kernel: raise it to

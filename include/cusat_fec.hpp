@@ -5,6 +5,10 @@
 //   lib/cusat_dsp/ldpc_decode.h                 (ldpc_decode)
 //   lib/cusat_dsp/cuda/demapper_kernel.cuh      (cuda::demapper_cuda)
 //   lib/cusat_dsp/cuda/bch_check_kernel.cuh     (cuda::bch_check_cuda)
+//   lib/cusat_dsp/rx_fec_chain.h                (rx_fec_chain, gpu_decode_budget)
+//   lib/cusat_dsp/rx_fec_pool.h                 (rx_fec_pool: declared when this
+//                                                header is included after the
+//                                                reference's acm_config.h)
 // compiles unchanged and links against libcusat_fec.so.
 //
 // Error behaviour mirrors the reference: a batch size outside 1..max_batch is
@@ -13,14 +17,20 @@
 // std::invalid_argument on a bad geometry, negative batch or null buffer
 // (bch_check_kernel.cu:17-18,28-33), and construction without a GPU aborts
 // (ldpc_decode.cc:33-40).
-#pragma once
+#ifndef CUSAT_FEC_HPP
+#define CUSAT_FEC_HPP
 
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 
+#include <chrono>
+#include <complex>
+#include <memory>
+#include <mutex>
 #include <stdexcept>
+#include <vector>
 
 #include "cusat_fec.h"
 
@@ -270,4 +280,248 @@ class ldpc_decode
     int max_batch_ = 0;
 };
 
+
+// Reference lib/cusat_dsp/rx_fec_chain.h:52-59.  The cap lives in the
+// library; chains share it through set_decode_budget.
+struct gpu_decode_budget {
+    cusat_decode_budget* h = nullptr;
+    explicit gpu_decode_budget(int cap_frames = -1)
+    {
+        const int rc = cusat_decode_budget_create(cap_frames, &h);
+        if (rc)
+            cusat_shim::die(rc, "gpu_decode_budget");
+    }
+    ~gpu_decode_budget() { cusat_decode_budget_destroy(h); }
+    gpu_decode_budget(const gpu_decode_budget&) = delete;
+    gpu_decode_budget& operator=(const gpu_decode_budget&) = delete;
+    static std::shared_ptr<gpu_decode_budget> make_default() { return std::make_shared<gpu_decode_budget>(-1); }
+    int cap() const
+    {
+        int32_t v[2];
+        cusat_decode_budget_info(h, v);
+        return v[0];
+    }
+    int in_flight() const
+    {
+        int32_t v[2];
+        cusat_decode_budget_info(h, v);
+        return v[1];
+    }
+};
+
+// Reference lib/cusat_dsp/rx_fec_chain.h:61-297 (the diagnostic flags are
+// accepted and ignored: they write files under /tmp in the reference).
+class rx_fec_chain
+{
+  public:
+    typedef std::complex<float> sym_t;
+
+    rx_fec_chain(fecframe_size_t framesize, code_rate_t rate, modulation_t constellation, int max_trials = 25,
+                 int cuda_max_batch = 64, int n_gpu_streams = 8, int micro_batch = 4)
+    {
+        const int rc = cusat_rx_chain_create((int)framesize, (int)rate, (int)constellation, max_trials,
+                                             cuda_max_batch, n_gpu_streams, micro_batch, &c_);
+        if (rc)
+            cusat_shim::die(rc, "rx_fec_chain");
+        owned_ = true;
+        init();
+    }
+    explicit rx_fec_chain(cusat_rx_chain* borrowed) : c_(borrowed) { init(); }
+    ~rx_fec_chain()
+    {
+        if (owned_)
+            cusat_rx_chain_destroy(c_);
+    }
+    rx_fec_chain(const rx_fec_chain&) = delete;
+    rx_fec_chain& operator=(const rx_fec_chain&) = delete;
+
+    bool submit_xfecframe(const sym_t* symbols, int n_symbols)
+    {
+        return ok(cusat_rx_chain_submit_xfecframe(c_, reinterpret_cast<const float*>(symbols), n_symbols),
+                  "submit_xfecframe") > 0;
+    }
+    int get_gse_output(uint8_t* out, int max_bytes)
+    {
+        const int n = ok(cusat_rx_chain_get_gse_output(c_, out, max_bytes), "get_gse_output");
+        const int k = cusat_rx_chain_gse_dfl_sizes(c_, nullptr, 0);
+        sizes_.resize((size_t)k);
+        cusat_rx_chain_gse_dfl_sizes(c_, sizes_.data(), k);
+        return n;
+    }
+    const std::vector<int>& gse_dfl_sizes() const { return sizes_; }
+    void reset() { ok(cusat_rx_chain_reset(c_), "reset"); }
+    void flush() { ok(cusat_rx_chain_flush(c_), "flush"); }
+    bool drain_completed() { return ok(cusat_rx_chain_drain_completed(c_), "drain_completed") > 0; }
+    void launch_partial() { ok(cusat_rx_chain_launch_partial(c_), "launch_partial"); }
+    void warmup() { ok(cusat_rx_chain_warmup(c_), "warmup"); }
+    void update_snr(float snr_db) { cusat_rx_chain_update_snr(c_, snr_db); }
+    void set_block_when_full(bool on) { cusat_rx_chain_set_block_when_full(c_, on ? 1 : 0); }
+    void set_diag_fec_bench(bool) {}
+    void set_diag_llr_histogram(bool) {}
+    void set_diag_ldpc_convergence(bool) {}
+    void set_cuda_mutex(std::mutex* mtx)
+    {
+        if (mtx)
+            cusat_rx_chain_set_launch_lock(c_, &lock_mutex, &unlock_mutex, mtx);
+        else
+            cusat_rx_chain_set_launch_lock(c_, nullptr, nullptr, nullptr);
+    }
+    void set_decode_budget(std::shared_ptr<gpu_decode_budget> b)
+    {
+        if (b) {
+            cusat_rx_chain_set_decode_budget(c_, b->h);
+            budget_ = std::move(b);
+        }
+    }
+    static bool frame_passes_fec_checks(int ldpc_trials_remaining, bool bch_valid)
+    {
+        return ldpc_trials_remaining >= 0 && bch_valid;
+    }
+
+    float snr_db() const { return (float)stat(7); }
+    float data_snr_db() const { return (float)stat(7); }
+    float precision() const { return (float)stat(8); }
+    uint64_t frame_count() const { return (uint64_t)stat(0); }
+    uint64_t frame_error_count() const { return (uint64_t)stat(1); }
+    uint64_t gpu_drop_count() const { return (uint64_t)stat(2); }
+    int gpu_inflight() const { return (int)stat(3); }
+    int gpu_pending_launch() const { return (int)stat(4); }
+    uint64_t force_drain_count() const { return (uint64_t)stat(5); }
+    int pending_count() const { return (int)stat(6); }
+    int batch_size() const { return info_[2]; }
+    int max_output_bytes() const { return info_[3]; }
+    std::chrono::steady_clock::time_point batch_start_time() const
+    {
+        return std::chrono::steady_clock::now() -
+               std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                   std::chrono::duration<double>(stat(10)));
+    }
+
+  private:
+    void init() { cusat_rx_chain_info(c_, info_); }
+    double stat(int i) const
+    {
+        double v[12];
+        cusat_rx_chain_stats(c_, v);
+        return v[i];
+    }
+    static int ok(int rc, const char* what)
+    {
+        if (rc < 0)
+            cusat_shim::die(rc, what);
+        return rc;
+    }
+    static void lock_mutex(void* m) { static_cast<std::mutex*>(m)->lock(); }
+    static void unlock_mutex(void* m) { static_cast<std::mutex*>(m)->unlock(); }
+
+    cusat_rx_chain* c_ = nullptr;
+    bool owned_ = false;
+    int32_t info_[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<int> sizes_;
+    std::shared_ptr<gpu_decode_budget> budget_;
+};
+
 }  // namespace cusat_dsp
+#endif  // CUSAT_FEC_HPP
+
+// The pool needs the reference's find_modcod (acm_config.h): it is declared
+// by whichever inclusion of this header follows acm_config.h.
+#if defined(INCLUDED_CUSAT_DSP_ACM_CONFIG_H) && !defined(CUSAT_FEC_HPP_POOL)
+#define CUSAT_FEC_HPP_POOL
+namespace cusat_dsp {
+
+// Reference lib/cusat_dsp/rx_fec_pool.h:25-140; MODCODs resolved with the
+// reference's find_modcod.  submit takes any layout type with a modcod
+// member (the reference's pl_layout).
+class rx_fec_pool
+{
+  public:
+    typedef std::complex<float> sym_t;
+
+    rx_fec_pool(fecframe_size_t framesize, const std::vector<uint8_t>& enabled_modcods, int max_trials = 25,
+                int cuda_max_batch = 64, int n_gpu_streams = 8, int micro_batch = 4)
+    {
+        std::vector<int32_t> triples;
+        for (uint8_t idx : enabled_modcods) {
+            const modcod_def_t* def = find_modcod(idx);
+            if (!def)
+                throw std::invalid_argument("Unknown modcod_idx: " + std::to_string(idx));
+            triples.push_back(idx);
+            triples.push_back((int32_t)def->constellation);
+            triples.push_back((int32_t)def->code_rate);
+        }
+        const int rc = cusat_rx_pool_create((int)framesize, triples.data(), (int)enabled_modcods.size(),
+                                            max_trials, cuda_max_batch, n_gpu_streams, micro_batch, &p_);
+        if (rc)
+            cusat_shim::die(rc, "rx_fec_pool");
+    }
+    ~rx_fec_pool() { cusat_rx_pool_destroy(p_); }
+    rx_fec_pool(const rx_fec_pool&) = delete;
+    rx_fec_pool& operator=(const rx_fec_pool&) = delete;
+
+    template <class Layout>
+    bool submit(const sym_t* symbols, int n_symbols, const Layout& pls)
+    {
+        return ok(cusat_rx_pool_submit(p_, reinterpret_cast<const float*>(symbols), n_symbols, (int)pls.modcod),
+                  "submit") > 0;
+    }
+    int get_gse_output(uint8_t* out, int max_bytes)
+    {
+        const int n = ok(cusat_rx_pool_get_gse_output(p_, out, max_bytes), "get_gse_output");
+        const int k = cusat_rx_pool_gse_dfl_sizes(p_, nullptr, 0);
+        sizes_.resize((size_t)k);
+        cusat_rx_pool_gse_dfl_sizes(p_, sizes_.data(), k);
+        return n;
+    }
+    const std::vector<int>& gse_dfl_sizes() const { return sizes_; }
+    void reset_all() { ok(cusat_rx_pool_reset_all(p_), "reset_all"); }
+    void warmup_all() { ok(cusat_rx_pool_warmup_all(p_), "warmup_all"); }
+    bool launch_stale(std::chrono::milliseconds max_age)
+    {
+        return ok(cusat_rx_pool_launch_stale(p_, (double)max_age.count()), "launch_stale") > 0;
+    }
+    bool drain_all_completed() { return ok(cusat_rx_pool_drain_all_completed(p_), "drain_all_completed") > 0; }
+    void finish_all_pending() { ok(cusat_rx_pool_finish_all_pending(p_), "finish_all_pending"); }
+    void set_diag_fec_bench(bool) {}
+    void set_diag_llr_histogram(bool) {}
+    void set_diag_ldpc_convergence(bool) {}
+    void set_cuda_mutex(std::mutex* mtx)
+    {
+        if (mtx)
+            cusat_rx_pool_set_launch_lock(p_, &lock_mutex, &unlock_mutex, mtx);
+        else
+            cusat_rx_pool_set_launch_lock(p_, nullptr, nullptr, nullptr);
+    }
+    void update_snr(uint8_t modcod, float snr_db) { cusat_rx_pool_update_snr(p_, modcod, snr_db); }
+    int max_output_bytes() const { return (int)stat(3); }
+    uint64_t total_frame_count() const { return (uint64_t)stat(0); }
+    uint64_t total_error_count() const { return (uint64_t)stat(1); }
+    bool modcod_counters(uint8_t modcod, uint64_t& frames, uint64_t& errors) const
+    {
+        return cusat_rx_pool_modcod_counters(p_, modcod, &frames, &errors) == 1;
+    }
+    uint64_t total_gpu_drop_count() const { return (uint64_t)stat(2); }
+    float data_snr_db() const { return (float)stat(4); }
+
+  private:
+    double stat(int i) const
+    {
+        double v[5];
+        cusat_rx_pool_stats(p_, v);
+        return v[i];
+    }
+    static int ok(int rc, const char* what)
+    {
+        if (rc < 0)
+            cusat_shim::die(rc, what);
+        return rc;
+    }
+    static void lock_mutex(void* m) { static_cast<std::mutex*>(m)->lock(); }
+    static void unlock_mutex(void* m) { static_cast<std::mutex*>(m)->unlock(); }
+
+    cusat_rx_pool* p_ = nullptr;
+    std::vector<int> sizes_;
+};
+
+}  // namespace cusat_dsp
+#endif  // pool
