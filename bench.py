@@ -2,7 +2,7 @@
 
 Workload (headline): normal FECFRAME 3/5 (s2_b5), 8PSK with interleave
 "210", 256 frames per step at Es/N0 6.0 dB (seeded synthetic traffic from
-this project's BCH/LDPC encoder, mapper and AWGN channel), fused soft demap
+this project's BCH/LDPC encoder, mapper and AWGN channel), soft demap
 + deinterleave -> layered min-sum LDPC decode (max 50 iterations, syndrome
 early exit) -> BCH syndrome check.  One step = one batch through the chain.
 
@@ -331,6 +331,25 @@ def main():
         iters.append(np.where(tr >= 0, T - tr, T))
     it = np.concatenate(iters)
     launch_ms = float(np.mean(launch))
+    # the chain's kernels one at a time (the same kernels rx_fec launches):
+    # demap into an LLR buffer, then the decoder, each bracketed by events
+    dmp = cs.demapper_cuda(wl["mod"], wl["rate"], wl["fs"], B)
+    dec = cs.ldpc_decode_cuda(wl["fs"], wl["rate"], T, B)
+    soft = torch.empty((B, ci["n_ldpc"]), dtype=torch.int16, device="cuda")
+    g_cap = cs.capped_llr_gain(wl["mod"], wl["rate"], wl["fs"], gain)
+    demap_t, dec_t = [], []
+    for i in range(N_BUFS + 1):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        dmp.demap_launch(d_sym[i % N_BUFS], B, n0, g_cap, soft, st)
+        e1.record(st)
+        dec.decode_launch_async(soft, B, st, hard, trials)
+        e2.record(st)
+        st.synchronize()
+        if i:  # first round warms the two objects up
+            demap_t.append(e0.elapsed_time(e1))
+            dec_t.append(e1.elapsed_time(e2))
+    demap_ms, dec_ms = float(np.mean(demap_t)), float(np.mean(dec_t))
 
     # max over ranks
     from cusat_gb300 import replicas
@@ -345,11 +364,17 @@ def main():
         return
 
     mi = cs.modcod_info(wl["mod"], wl["rate"], wl["fs"])
+    # algorithmic HBM bytes: the chain reads symbols (8 B each) and writes
+    # hard bits, iteration counts and BCH flags; the decoder reads the LLRs
+    # (2 B per bit) and writes hard bits and counts; the demap reads symbols
+    # and writes LLRs
     per_launch_bytes = B * (mi["xfecframe_len"] * 8 + ci["k_ldpc"] // 8 + 12)
+    dec_bytes = B * (2 * ci["n_ldpc"] + ci["k_ldpc"] // 8 + 4)
+    demap_bytes = B * (mi["xfecframe_len"] * 8 + 2 * ci["n_ldpc"])
     launch_s = launch_ms * 1e-3
     peaks = load_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = per_launch_bytes / launch_s / 1e9
+    achieved = dec_bytes / (dec_ms * 1e-3) / 1e9
     traffic, prof = None, {}
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "dram_traffic.json"))).get(args.workload, {})
@@ -365,7 +390,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16",
         "data": f"synthetic (seeded BCH/LDPC-encoded {wl['mod_name']} frames, AWGN at Es/N0 {wl['esn0_db']} dB)",
-        "config": {"workload": f"{wl['name']} ({wl['code']}), {B} frames, Es/N0 {wl['esn0_db']} dB: fused demap + "
+        "config": {"workload": f"{wl['name']} ({wl['code']}), {B} frames, Es/N0 {wl['esn0_db']} dB: demap + "
                                f"deinterleave -> layered min-sum LDPC (max {T} it) -> BCH check",
                    "frames": B, "max_trials": T, "esn0_db": wl["esn0_db"], "decoder": "plain offset min-sum",
                    "parallelism": f"replicas x{world}; {pipe} chains on {pipe} streams, consecutive batches "
@@ -376,23 +401,31 @@ def main():
                    "frames_failed": int(np.sum(it >= T))},
         "e2e": {"value": e2e, "unit": "Gbit/s", "h2d_bytes_per_step": int(bufs[0].nbytes),
                 "d2h_bytes_per_step": int(B * (k_bytes + 8))},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic, "algorithmic_bytes": per_launch_bytes,
-                     "note": "algorithmic HBM bytes per launch (8 B/symbol in, k/8 + 12 B/frame out) over the "
-                             "fused chain's launch time (CUDA events), peak = measured copy bandwidth (of measured); "
-                             "traffic = DRAM bytes of one decoder launch from the ncu capture in "
-                             "profiles/ (null when none was taken for this workload); the decoder is bound "
-                             "by the integer ALU pipe (onchip)"},
-        "onchip": {"edge_iterations_per_s": edge_iters / launch_s,
+        "roofline": {"bound": "hbm", "kernel": "ldpc_layered_kernel (decoder)", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                     "algorithmic_bytes": dec_bytes, "launch_ms": dec_ms,
+                     "note": "dominant kernel = the decoder: algorithmic HBM bytes per launch (2 B per LLR in, "
+                             "k/8 + 4 B per frame out) over its launch time (CUDA events on its stream), peak "
+                             "= measured copy bandwidth (of measured); traffic = DRAM bytes of one decoder "
+                             "launch from the ncu capture in profiles/ (null when none was taken for this "
+                             "workload); the decoder is bound by integer issue (onchip), not HBM",
+                     "kernels": {
+                         "demap": {"launch_ms": demap_ms, "algorithmic_bytes": demap_bytes,
+                                   "achieved_gbs": demap_bytes / (demap_ms * 1e-3) / 1e9,
+                                   "frac": demap_bytes / (demap_ms * 1e-3) / 1e9 / hbm_peak},
+                         "decoder": {"launch_ms": dec_ms, "algorithmic_bytes": dec_bytes},
+                         "chain": {"launch_ms": launch_ms, "algorithmic_bytes": per_launch_bytes,
+                                   "achieved_gbs": per_launch_bytes / launch_s / 1e9}}},
+        "onchip": {"edge_iterations_per_s": edge_iters / (dec_ms * 1e-3),
                    "alu_pipe_pct_ncu": prof.get("alu_pipe_pct"), "issue_active_pct_ncu": prof.get("issue_active_pct"),
-                   "smem_app_bytes_per_s": 4.0 * edge_iters / launch_s,
+                   "smem_app_bytes_per_s": 4.0 * edge_iters / (dec_ms * 1e-3),
                    "note": "mean iterations x Tanner edges x frames per launch; 4 B of shared-memory APP "
                            "traffic per edge-iteration (gather + scatter), messages 2 B in L2"},
         "cpu_baseline": {"value": cpu_value, "unit": "Gbit/s", "cores": threads, "kind": "port",
                          "sample": f"{n_cpu} frames of the workload ({n_cpu // B} batches) through the C oracle "
                                    f"(demap + decode + BCH), {cpu_s:.1f} s on {threads} threads"},
         "clocks": clk,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,  # demap, decoder, BCH check per step
         "wall_s": wall,
     }
     print(json.dumps(line), flush=True)
@@ -617,7 +650,7 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
         "data": "synthetic (seeded mixed-MODCOD frames from this project's encoder and mapper, AWGN at each "
                 "MODCOD's threshold + 0.5 dB)",
         "config": {"workload": "mixed: 1024 frames of 10 MODCODs (64APSK 32/45 for S2X 64APSK 2/3), 70% normal "
-                               "/ 30% short, fused demap -> decode (max 50 it) -> BCH, one CUDA graph replay "
+                               "/ 30% short, demap -> decode (max 50 it) -> BCH, one CUDA graph replay "
                                "per step (tuned grid and class order)",
                    "frames": n, "max_trials": T, "kernel_classes": n_classes, "learned_weights": bool(args.learned),
                    "parallelism": f"replicas x{world}; {S} graphs on {S} streams, consecutive batches overlap",
@@ -636,7 +669,7 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
                          "sample": f"{reps} x the first {n_cpu} frames through the C oracle, {cpu_s:.1f} s on "
                                    f"{threads} threads"},
         "clocks": clk,
-        "gpu_launches": args.steps * (n_classes + 1),
+        "gpu_launches": args.steps * (n_classes + 2),  # demap, one decoder per class, BCH
     }), flush=True)
 
 
@@ -764,7 +797,7 @@ def learned_main(args, torch, cs, rank, local_rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["learned20"]["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
         "data": "synthetic (seeded BCH/LDPC-encoded QPSK frames, AWGN at Es/N0 0.56 dB)",
-        "config": {"workload": "normal 1/3 QPSK (s2_b2), 256 frames at its threshold 0.56 dB: fused demap -> "
+        "config": {"workload": "normal 1/3 QPSK (s2_b2), 256 frames at its threshold 0.56 dB: demap -> "
                                "learned min-sum (max 20 it) vs plain (max 50 it) -> BCH",
                    "learned": res["learned20"], "plain": res["plain50"],
                    "speedup": res["learned20"]["gbit_s"] / res["plain50"]["gbit_s"]},
@@ -777,7 +810,7 @@ CODES = [("qpsk1/4", 0), ("qpsk1/2", 1), ("qpsk1/2", 0), ("8psk3/5", 1), ("8psk3
 
 def codes_main(args, torch, cs, rank, local_rank, world):
     """One MODCOD per kernel class (circulant slots per layer x lanes): 256
-    frames at threshold + 0.5 dB through the fused chain, median of `steps`
+    frames at threshold + 0.5 dB through the receive chain, median of `steps`
     single launches (CUDA events) after `warmup`; value = the headline
     class's Gbit/s, the others in config.codes."""
     from cusat_gb300 import traffic

@@ -15,7 +15,7 @@ arguments and result conventions of the reference's C++ classes for the path:
   rx_fec_pool       lib/cusat_dsp/rx_fec_pool.h:25-140
   gpu_decode_budget lib/cusat_dsp/rx_fec_chain.h:52-59
 
-plus ``rx_fec`` (one MODCOD's fused demap -> decode -> BCH chain).
+plus ``rx_fec`` (one MODCOD's demap -> decode -> BCH chain).
 
 Device buffers are torch CUDA tensors (or raw device addresses as int);
 host buffers are numpy arrays.  Streams are torch.cuda.Stream objects, raw
@@ -308,7 +308,7 @@ class bch_check_cuda:
 
 
 class rx_fec:
-    """One MODCOD's receive chain: fused demap + deinterleave + LDPC decode,
+    """One MODCOD's receive chain: demap + deinterleave, LDPC decode,
     then the BCH check (replaces rx_fec_chain::launch_slot_gpu's launch
     sequence, lib/cusat_dsp/rx_fec_chain.cc:361-505)."""
 
@@ -346,7 +346,7 @@ class rx_fec:
 
 class batch:
     """Mixed-MODCOD batch decoder: frames of any of `modcods` ((modulation,
-    rate, frame size) triples) in one launch sequence (fused demap -> decode
+    rate, frame size) triples) in one launch sequence (demap -> decode
     -> BCH), optionally captured into a CUDA graph.  No counterpart in the
     reference (one chain per MODCOD, lib/cusat_dsp/rx_fec_pool.cc:48-87)."""
 

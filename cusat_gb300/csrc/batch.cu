@@ -167,9 +167,10 @@ int stage(cusat_batch* b, const cusat_frame* frames, int n)
 
 // Launch sequence for n staged frames whose descriptors are (or, with
 // `copy`, are first copied from the pinned staging arrays) at
-// d_frames/d_bch/d_demap: the demap of every frame over the whole grid,
-// then one decoder launch per kernel class on its own stream, then the BCH
-// check of every frame.
+// d_frames/d_bch/d_demap: the demap of every frame in one launch (per-class
+// demap launches on the class streams measured slower: their overlap with
+// decoding does not pay for eleven smaller grids), then one decoder launch
+// per kernel class on its own stream, then the BCH check of every frame.
 int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, cusat::BchFrame* d_bch,
             cusat::DemapFrame* d_demap, bool copy)
 {

@@ -23,7 +23,7 @@ using namespace cusat_internal;
 
 namespace {
 
-// Decoder engine shared by the plain decoder and the fused chain.
+// Decoder engine shared by the plain decoder and the receive chain.
 struct Engine {
     const cusat::CodePlan* plan = nullptr;
     DevPlan dp;
@@ -460,7 +460,7 @@ int cusat_bch_check_launch(cusat_bch_checker* c, const uint8_t* codewords_dev, i
 }
 
 // --------------------------------------------------------------------------
-// Fused receive chain
+// Receive chain: demap -> decode -> BCH
 // --------------------------------------------------------------------------
 
 int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials, int max_batch,

@@ -4,48 +4,69 @@
 
 namespace cusat {
 
-// One thread per symbol (grid.y = frame), points staged in shared memory.
-// Reference cuda/demapper_kernel.cu:31-184 (same arithmetic as the decoder's
-// fused prologue: demap_symbol).
-__global__ void __launch_bounds__(256) demap_kernel(DevDemap d, const float2* __restrict__ sym,
-                                                   int16_t* __restrict__ out, float noise_var,
-                                                   float llr_gain)
+constexpr int kDemapThreads = 256, kDemapSpan = 4;  // symbols per thread per pass
+
+// One MODCOD: grid.y = frame, each thread kDemapSpan symbols spaced a block
+// apart, points staged in shared memory.  Reference
+// cuda/demapper_kernel.cu:31-184.
+template <int KIND, int NM>
+__global__ void __launch_bounds__(kDemapThreads) demap_kernel(DevDemap d, const float2* __restrict__ sym,
+                                                             int16_t* __restrict__ out, float noise_var,
+                                                             float llr_gain)
 {
     __shared__ float2 pts[256];
-    if (d.kind == 2)
+    if (KIND == 2) {
         for (int k = threadIdx.x; k < d.n_points; k += blockDim.x)
             pts[k] = d.points[k];
-    __syncthreads();
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+        __syncthreads();
+    }
     const int f = blockIdx.y;
-    if (j >= d.interleaved_len)
-        return;
-    const float2 s = __ldcs(sym + (size_t)f * d.xfec + j);
-    int pos[8];
-    int16_t l[8];
-    const int nb = demap_symbol(d, pts, s.x, s.y, j, noise_var, llr_gain, pos, l);
-    int16_t* o = out + (size_t)f * d.fec_len;
-#pragma unroll
-    for (int b = 0; b < 8; b++)
-        if (b < nb && pos[b] < d.fec_len)
-            o[pos[b]] = l[b];
+    demap_span<KIND, NM, kDemapSpan>(d, pts, sym + (size_t)f * d.xfec, out + (size_t)f * d.fec_len,
+                                     blockIdx.x * kDemapThreads * kDemapSpan + threadIdx.x, kDemapThreads,
+                                     noise_var, llr_gain);
+}
+
+template <int KIND, int NM>
+void launch_demap_kind(const DevDemap& d, const float2* sym, int batch, float noise_var, float llr_gain,
+                       int16_t* out, cudaStream_t stream)
+{
+    const int per_block = kDemapThreads * kDemapSpan;
+    for (int f0 = 0; f0 < batch; f0 += 65535) {
+        dim3 grid((d.interleaved_len + per_block - 1) / per_block, batch - f0 < 65535 ? batch - f0 : 65535);
+        demap_kernel<KIND, NM><<<grid, kDemapThreads, 0, stream>>>(d, sym + (size_t)f0 * d.xfec,
+                                                                  out + (size_t)f0 * d.fec_len, noise_var,
+                                                                  llr_gain);
+    }
 }
 
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream)
 {
-    for (int f0 = 0; f0 < batch; f0 += 65535) {
-        dim3 grid((d.interleaved_len + 255) / 256, batch - f0 < 65535 ? batch - f0 : 65535);
-        demap_kernel<<<grid, 256, 0, stream>>>(d, reinterpret_cast<const float2*>(sym) + (size_t)f0 * d.xfec,
-                                               out + (size_t)f0 * d.fec_len, noise_var, llr_gain);
-    }
+    const float2* s = reinterpret_cast<const float2*>(sym);
+    if (d.kind == 0)
+        launch_demap_kind<0, 0>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.kind == 1)
+        launch_demap_kind<1, 0>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_points != 1 << d.n_mod)
+        launch_demap_kind<2, 0>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_mod == 3)
+        launch_demap_kind<2, 3>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_mod == 4)
+        launch_demap_kind<2, 4>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_mod == 5)
+        launch_demap_kind<2, 5>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_mod == 6)
+        launch_demap_kind<2, 6>(d, s, batch, noise_var, llr_gain, out, stream);
+    else
+        launch_demap_kind<2, 0>(d, s, batch, noise_var, llr_gain, out, stream);
     return (int)cudaGetLastError();
 }
 
 // Mixed batch: grid.y = frame, each frame's MODCOD parameters (and points)
-// staged in shared memory, blocks stride over the frame's symbols.
-__global__ void __launch_bounds__(256) demap_mixed_kernel(const DevDemap* __restrict__ demaps,
-                                                         const DemapFrame* __restrict__ frames)
+// staged in shared memory, blocks stride over the frame's symbols; the
+// frame's kind and bit count are uniform over the block.
+__global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDemap* __restrict__ demaps,
+                                                                   const DemapFrame* __restrict__ frames)
 {
     __shared__ float2 pts[256];
     __shared__ DevDemap d;
@@ -57,25 +78,28 @@ __global__ void __launch_bounds__(256) demap_mixed_kernel(const DevDemap* __rest
         for (int k = threadIdx.x; k < d.n_points; k += blockDim.x)
             pts[k] = d.points[k];
     __syncthreads();
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < d.interleaved_len; j += gridDim.x * blockDim.x) {
-        const float2 s = __ldcs(fr.sym + j);
-        int pos[8];
-        int16_t l[8];
-        const int nb = demap_symbol(d, pts, s.x, s.y, j, fr.noise_var, fr.llr_gain, pos, l);
-#pragma unroll
-        for (int b = 0; b < 8; b++)
-            if (b < nb && pos[b] < d.fec_len)
-                fr.out[pos[b]] = l[b];
+    const bool full = d.n_points == 1 << d.n_mod;  // 2^n_mod points: the specialised log-MAP applies
+    const int sel = d.kind == 2 ? 2 * 16 + (full && d.n_mod >= 4 && d.n_mod <= 6 ? d.n_mod : 0) : d.kind * 16;
+    const int per_block = kDemapThreads * kDemapSpan;
+    for (int j0 = blockIdx.x * per_block + threadIdx.x; j0 - (int)threadIdx.x < d.interleaved_len;
+         j0 += gridDim.x * per_block) {
+        switch (sel) {
+        case 0: demap_span<0, 0, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        case 16: demap_span<1, 0, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        case 36: demap_span<2, 4, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        case 37: demap_span<2, 5, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        case 38: demap_span<2, 6, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        default: demap_span<2, 0, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        }
     }
 }
 
 int launch_demap_mixed(const DevDemap* demaps, const DemapFrame* frames, int n, int max_len, cudaStream_t stream)
 {
-    // 4 symbols per thread for the longest frame: about 32 blocks per
-    // normal-frame QPSK frame, 128 threads' worth of work per block
+    const int per_block = kDemapThreads * kDemapSpan;
     for (int f0 = 0; f0 < n; f0 += 65535) {
-        dim3 grid((max_len + 1023) / 1024, n - f0 < 65535 ? n - f0 : 65535);
-        demap_mixed_kernel<<<grid, 256, 0, stream>>>(demaps, frames + f0);
+        dim3 grid((max_len + per_block - 1) / per_block, n - f0 < 65535 ? n - f0 : 65535);
+        demap_mixed_kernel<<<grid, kDemapThreads, 0, stream>>>(demaps, frames + f0);
     }
     return (int)cudaGetLastError();
 }

@@ -83,55 +83,69 @@ __device__ __forceinline__ float dm_log(float x)
     return __fmaf_rn((float)e, 0.693147180559945309f, l);
 }
 
-// LLRs of symbol j.  QPSK: 2 LLRs at positions 2j, 2j+1 (no interleaver);
-// 8PSK: formula after the -pi/8 rotation; APSK: log-MAP over the points
-// (pts in shared memory).  Writes n_mod (pos, llr) pairs; pos >= fec_len is
-// dropped by the caller.  Reference: cuda/demapper_kernel.cu:53-183.
-__device__ __forceinline__ int demap_symbol(const DevDemap& d, const float2* pts, float re, float im,
-                                            int j, float noise_var, float llr_gain, int* pos,
-                                            int16_t* llr)
+// LLRs of symbol j, written to their deinterleaved positions (pos >= the
+// frame length is dropped).  Reference: cuda/demapper_kernel.cu:53-183.
+//
+// QPSK: 2 LLRs at 2j, 2j+1 (no interleaver).
+__device__ __forceinline__ void demap_qpsk(const DevDemap& d, float re, float im, int j, float noise_var,
+                                           int16_t* out)
 {
-    if (d.kind == 0) {
-        const float scalar = __fdiv_rn(2.0f * 1.4142135623730951f, noise_var);
-        pos[0] = 2 * j;
-        pos[1] = 2 * j + 1;
-        llr[0] = llr_round(__fmul_rn(re, scalar));
-        llr[1] = llr_round(__fmul_rn(im, scalar));
-        if (2 * j + 1 >= d.fec_len)
-            pos[0] = pos[1] = d.fec_len;  // dropped together, like the reference
-        return 2;
-    }
-    if (d.kind == 1) {
-        const float C8 = 0.92387953251128676f, S8 = 0.38268343236508977f;
-        const float R2 = 0.70710678118654752f;
-        const float DIST = 2.0f * 0.38268343236508977f;
-        const float cr = __fmaf_rn(re, C8, __fmul_rn(im, S8));
-        const float ci = __fmaf_rn(-re, S8, __fmul_rn(im, C8));
-        const float scale = __fmul_rn(DIST, llr_gain);
-        llr[0] = llr_round(__fmul_rn(__fmul_rn(R2, __fsub_rn(fabsf(cr), fabsf(ci))), scale));
-        llr[1] = llr_round(__fmul_rn(cr, scale));
-        llr[2] = llr_round(__fmul_rn(ci, scale));
-        pos[0] = (int)d.col[0] + j;
-        pos[1] = (int)d.col[1] + j;
-        pos[2] = (int)d.col[2] + j;
-        return 3;
-    }
-    const int nm = d.n_mod;
-    float mn0[8], mn1[8], s0[8], s1[8];
+    const float scalar = __fdiv_rn(2.0f * 1.4142135623730951f, noise_var);
+    if (2 * j + 1 >= d.fec_len)
+        return;  // both dropped together, like the reference
+    out[2 * j] = llr_round(__fmul_rn(re, scalar));
+    out[2 * j + 1] = llr_round(__fmul_rn(im, scalar));
+}
+
+// 8PSK: formula after the -pi/8 rotation.
+__device__ __forceinline__ void demap_8psk(const DevDemap& d, float re, float im, int j, float llr_gain,
+                                           int16_t* out)
+{
+    const float C8 = 0.92387953251128676f, S8 = 0.38268343236508977f;
+    const float R2 = 0.70710678118654752f;
+    const float DIST = 2.0f * 0.38268343236508977f;
+    const float cr = __fmaf_rn(re, C8, __fmul_rn(im, S8));
+    const float ci = __fmaf_rn(-re, S8, __fmul_rn(im, C8));
+    const float scale = __fmul_rn(DIST, llr_gain);
+    const int16_t l[3] = {llr_round(__fmul_rn(__fmul_rn(R2, __fsub_rn(fabsf(cr), fabsf(ci))), scale)),
+                          llr_round(__fmul_rn(cr, scale)), llr_round(__fmul_rn(ci, scale))};
 #pragma unroll
-    for (int b = 0; b < 8; b++) {
+    for (int b = 0; b < 3; b++) {
+        const int p = (int)d.col[b] + j;
+        if (p < d.fec_len)
+            out[p] = l[b];
+    }
+}
+
+// APSK: log-MAP over the points (pts in shared memory), NM bits per symbol
+// (0: d.n_mod at run time; a compile-time NM resolves every label-bit test
+// and bit loop, same arithmetic).  UNROLL: point loops unrolled by 16 (one
+// MODCOD per kernel; a kernel that switches between MODCODs stays compact).
+template <int NM, bool UNROLL>
+__device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pts, float re, float im, int j,
+                                             float llr_gain, int16_t* out)
+{
+    constexpr int MB = NM ? NM : 8;
+    const int nm = NM ? NM : d.n_mod;
+    // a specialised call has exactly 2^NM points (checked by its launcher):
+    // unrolled by 16, the label bits below bit 4 are compile-time constants
+    const int np = NM ? (1 << NM) : d.n_points;
+    float mn0[MB], mn1[MB], s0[MB], s1[MB];
+#pragma unroll
+    for (int b = 0; b < MB; b++) {
         mn0[b] = 1e30f;
         mn1[b] = 1e30f;
         s0[b] = 0.0f;
         s1[b] = 0.0f;
     }
-    for (int i = 0; i < d.n_points; i++) {
+#pragma unroll (NM && UNROLL ? 16 : 1)
+    for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
         const float dd = __fmaf_rn(dr, dr, __fmul_rn(di, di));
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
-            if (b < nm) {
+        for (int b = 0; b < MB; b++) {
+            if (NM || b < nm) {
                 if (i & (1 << (nm - 1 - b))) {
                     if (dd < mn1[b]) mn1[b] = dd;
                 } else {
@@ -141,13 +155,14 @@ __device__ __forceinline__ int demap_symbol(const DevDemap& d, const float2* pts
         }
     }
     const float scale = __fmul_rn(llr_gain, 0.25f);
-    for (int i = 0; i < d.n_points; i++) {
+#pragma unroll (NM && UNROLL ? 16 : 1)
+    for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
         const float dd = __fmaf_rn(dr, dr, __fmul_rn(di, di));
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
-            if (b < nm) {
+        for (int b = 0; b < MB; b++) {
+            if (NM || b < nm) {
                 if (i & (1 << (nm - 1 - b))) {
                     const float delta = __fmul_rn(__fsub_rn(dd, mn1[b]), scale);
                     if (delta < 16.0f) s1[b] = __fadd_rn(s1[b], dm_exp_neg(delta));
@@ -160,15 +175,42 @@ __device__ __forceinline__ int demap_symbol(const DevDemap& d, const float2* pts
     }
     const float half_gain = __fmul_rn(llr_gain, 0.5f);
 #pragma unroll
-    for (int b = 0; b < 8; b++) {
-        if (b < nm) {
+    for (int b = 0; b < MB; b++) {
+        if (NM || b < nm) {
             const float corr = __fmul_rn(2.0f, __fsub_rn(dm_log(fmaxf(s0[b], 1e-30f)),
                                                          dm_log(fmaxf(s1[b], 1e-30f))));
-            llr[b] = llr_round(__fmaf_rn(__fsub_rn(mn1[b], mn0[b]), half_gain, corr));
-            pos[b] = (int)d.col[b] + j;
+            const int p = (int)d.col[b] + j;
+            if (p < d.fec_len)
+                out[p] = llr_round(__fmaf_rn(__fsub_rn(mn1[b], mn0[b]), half_gain, corr));
         }
     }
-    return nm;
+}
+
+// Demaps the symbols j0, j0 + step, ... (U of them, those inside the frame)
+// of one frame: all U loads first (memory parallelism for the formula
+// kinds), then each symbol.  KIND 0 QPSK, 1 8PSK, 2 log-MAP with NM bits.
+template <int KIND, int NM, int U, bool UNROLL = true>
+__device__ __forceinline__ void demap_span(const DevDemap& d, const float2* pts, const float2* sym, int16_t* out,
+                                           int j0, int step, float noise_var, float llr_gain)
+{
+    float2 s[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int j = j0 + u * step;
+        s[u] = j < d.interleaved_len ? __ldcs(sym + j) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int j = j0 + u * step;
+        if (j >= d.interleaved_len)
+            break;
+        if (KIND == 0)
+            demap_qpsk(d, s[u].x, s[u].y, j, noise_var, out);
+        else if (KIND == 1)
+            demap_8psk(d, s[u].x, s[u].y, j, llr_gain, out);
+        else
+            demap_logmap<NM, UNROLL>(d, pts, s[u].x, s[u].y, j, llr_gain, out);
+    }
 }
 
 }  // namespace cusat

@@ -1,12 +1,12 @@
 // Frame-at-a-time receive chain and its per-MODCOD pool: the reference's
 // rx_fec_chain (lib/cusat_dsp/rx_fec_chain.cc:41-627) and rx_fec_pool
 // (lib/cusat_dsp/rx_fec_pool.cc:15-270) with the same submit / drain / output
-// semantics, over the fused kernels of this library.
+// semantics, over the receive-chain kernels of this library.
 //
 // Where the reference launches demap, LDPC and BCH per micro-batch on one of
 // n streams, copies every frame's hard bits to pinned memory and descrambles
 // and parses each BBFRAME on the host, a slot here is one H2D copy of its
-// symbols, the fused demap + decode launch, the BCH check and the device-side
+// symbols, the demap and decode launches, the BCH check and the device-side
 // BB stage, which writes only the packed GSE data fields, their lengths and
 // the per-frame verdicts into the slot's pinned memory.  The host's drain is
 // a counter update and one memcpy per slot.
@@ -64,7 +64,7 @@ struct Slot {
     int stream = -1, n_frames = 0;
 };
 
-// One stream with its own fused chain and device buffers.
+// One stream with its own receive chain and device buffers.
 struct Lane {
     cusat_rx_fec* rx = nullptr;
     cudaStream_t stream = nullptr;
@@ -123,7 +123,7 @@ void release_budget(cusat_rx_chain* c, int n)
         c->budget->in_flight.fetch_sub(n, std::memory_order_relaxed);
 }
 
-// rx_fec_chain::launch_slot_gpu (rx_fec_chain.cc:361-505): symbols up, fused
+// rx_fec_chain::launch_slot_gpu (rx_fec_chain.cc:361-505): symbols up,
 // demap + decode, BCH, BB stage, completion event; the noise variance and
 // gain are the chain's at launch time.
 int launch_slot(cusat_rx_chain* c, Slot& s)

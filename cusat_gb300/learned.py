@@ -168,7 +168,7 @@ class ChannelPool:
         sym += sigma * torch.randn(sym.shape, device="cuda", generator=self.gen)
         llr = torch.empty((batch, self.n), dtype=torch.int16, device="cuda")
         gain = min(4.0 / n0, 1000.0)
-        # the fused chain caps the gain the same way (demapper_kernel.cu:283-291)
+        # the receive chain caps the gain the same way (demapper_kernel.cu:283-291)
         self.dm.demap_launch(sym, batch, n0, self.dm.capped_llr_gain(gain), llr, st)
         return sym, llr, cw, n0, gain
 
@@ -234,7 +234,7 @@ def train(name, framesize, n_iter=20, esn0_grid=None, n_frames=100000, batch=128
 
 def frame_errors(name, framesize, esn0_db, n_iter, weights, n_frames, batch=256, seed=7, min_errors=None,
                  stream=None):
-    """Frame error rate of the integer decoder (fused chain) with `weights`
+    """Frame error rate of the integer decoder (receive chain) with `weights`
     (None = plain) at `n_iter` maximum iterations on fresh noisy frames.
     A frame is in error when its decoded k_ldpc bits differ from the sent
     ones.  Stops early after `min_errors` frame errors.  Returns a dict."""

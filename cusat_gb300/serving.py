@@ -9,7 +9,7 @@ AWGN.  A frame occupies plframe_symbols = 90 + 90 S + 36 floor((S - 1) / 16)
 symbols on the air with pilots, S = XFECFRAME symbols / 90 (the reference's
 framing/plframe.cc:209-226).  The noisy symbols come from a pool generated
 once per (MODCOD, frame size) and kept on the device; LLRs are produced on
-the device by the decoder's fused demapper.
+the device by the batch's demap kernel.
 """
 import numpy as np
 

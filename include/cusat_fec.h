@@ -160,14 +160,15 @@ int cusat_bch_check_launch(cusat_bch_checker* bc, const uint8_t* codewords_dev,
                            int32_t* valid_out, uint8_t* rem_out, int batch, void* stream);
 
 /* ---------------------------------------------------------------------- */
-/* Fused receive chain for one MODCOD                                      */
+/* Receive chain for one MODCOD                                            */
 /* ---------------------------------------------------------------------- */
 
 typedef struct cusat_rx_fec cusat_rx_fec;
 
-/* One MODCOD's demap + deinterleave -> LDPC decode -> BCH check, fused in
- * one decoder launch (the demap runs in the decoder's prologue, the
- * LLRs never leave shared memory) followed by the BCH check.  Replaces the
+/* One MODCOD's demap + deinterleave -> LDPC decode -> BCH check as one
+ * launch sequence on one stream: the demap over the whole grid into the
+ * object's LLR scratch in device memory, the persistent decoder, the BCH
+ * check.  Replaces the
  * per-slot launch sequence of rx_fec_chain::launch_slot_gpu
  * (lib/cusat_dsp/rx_fec_chain.cc:361-505). */
 int cusat_rx_fec_create(int modulation, int rate, int framesize, int max_trials, int max_batch,
@@ -205,7 +206,7 @@ typedef struct {
 /* No counterpart in the reference, which builds one chain per MODCOD and
  * flushes on every MODCOD change (lib/cusat_dsp/rx_fec_pool.cc:48-87).  A
  * batch decodes frames of any of the given MODCODs (modcods: n triples
- * modulation, rate, frame size) in one launch sequence: fused demap ->
+ * modulation, rate, frame size) in one launch sequence: demap ->
  * decode -> BCH; each frame's results equal those of a single-MODCOD
  * cusat_rx_fec launch on the same symbols. */
 int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, int max_frames,
