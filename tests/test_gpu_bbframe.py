@@ -79,3 +79,32 @@ def test_receive_chain_end_to_end(cuda):
     L, Off, o = lengths.cpu().numpy(), offsets.cpu().numpy(), out.cpu().numpy()
     for f, p in enumerate(payloads):
         assert L[f] == len(p) and (o[Off[f]:Off[f] + L[f]] == p).all()
+
+
+@pytest.mark.parametrize("fs,rate", [(NORMAL, E.RATE_1_2), (SHORT, E.RATE_1_2)])
+def test_kernel_header_rejections(cuda, fs, rate):
+    """The reference parser tests' header cases (valid, largest and empty
+    DFL, every single-bit header error, oversize and fractional DFL, non-GSE
+    TS/GS) through the device BB stage: the expected lengths and bytes."""
+    from test_oracle_bb import header_cases
+    torch = cuda
+    ci = cs.code_info(fs, rate)
+    kbch, stride = ci["k_bch"] // 8, ci["k_ldpc"] // 8
+    cases = header_cases(kbch, np.random.default_rng(2))
+    B = len(cases)
+    hard = np.zeros((B, stride), np.uint8)
+    hard[:, :kbch] = np.stack([c[0] for c in cases])
+    want = np.array([c[1] for c in cases])
+    trials = np.full(B, 5, np.int32)
+    valid = np.ones(B, np.int32)
+    out_o, len_o, off_o = O.bb_extract(hard, kbch, trials, valid, B * kbch)
+    assert (len_o == want).all()
+    d = [torch.from_numpy(a).cuda() for a in (hard, trials, valid)]
+    out = torch.zeros(B * kbch, dtype=torch.uint8, device="cuda")
+    lengths = torch.zeros(B, dtype=torch.int32, device="cuda")
+    offsets = torch.zeros(B + 1, dtype=torch.int32, device="cuda")
+    cs.bb_extractor(fs, rate).extract(d[0], stride, d[1], d[2], B, out, B * kbch, lengths, offsets,
+                                      torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    assert (lengths.cpu().numpy() == want).all()
+    assert (out.cpu().numpy()[:off_o[B]] == out_o).all()

@@ -70,3 +70,91 @@ def test_builder_and_extraction_match_reference(fs, rate):
         expect = lengths[f] if lengths[f] <= room - used else 0
         assert l2[f] == expect and o2[f] == used
         used += expect
+
+
+# ---- known answers of the reference's own tests, without the reference tree ----
+
+def crc8_dvbs2(data):
+    """CRC-8/DVB-S2: polynomial 0xD5, init 0, no reflection (EN 302 307-1 5.1.6)."""
+    reg = 0
+    for b in bytes(data):
+        reg ^= b
+        for _ in range(8):
+            reg = ((reg << 1) ^ 0xD5) & 0xFF if reg & 0x80 else (reg << 1) & 0xFF
+    return reg
+
+
+def bbframe(kbch, dfl_bits, ts_gs=0, rng=None, payload=None):
+    """A scrambled BBFRAME with the given header fields (MATYPE-1 = TS/GS in
+    its top bits, SIS, CCM, RO 0.35; CRC-8 over the first 9 bytes) and random
+    or given data field (reference lib/qa_bbframe_parser.cc:27-43)."""
+    rng = rng or np.random.default_rng(0)
+    f = rng.integers(0, 256, kbch, dtype=np.uint8)
+    f[0] = (ts_gs << 6) | (1 << 5) | (1 << 4)
+    f[1] = 0
+    f[2:4] = 0
+    f[4], f[5] = (dfl_bits >> 8) & 0xFF, dfl_bits & 0xFF
+    f[6:9] = 0
+    f[9] = crc8_dvbs2(f[:9])
+    if payload is not None:
+        f[10:10 + len(payload)] = payload
+    return f ^ O.bb_prbs(kbch)
+
+
+def test_crc8_and_prbs_known_answers():
+    # lib/qa_crc8.cc:13-19, lib/qa_bb_scrambler.cc:40-46
+    assert crc8_dvbs2(b"123456789") == 0xBC and crc8_dvbs2(b"") == 0
+    assert O.bb_prbs(8)[0] == 0x03
+    # figure 5's register, bit-serial: stage 14 xor stage 15 fed back to stage 1
+    st = [0] + [int(c) for c in "100101010000000"]
+    bits = []
+    for _ in range(8 * 64):
+        b = st[14] ^ st[15]
+        st = [0, b] + st[1:15]
+        bits.append(b)
+    ref = np.packbits(np.array(bits, np.uint8))
+    assert (O.bb_prbs(64) == ref).all()
+
+
+def header_cases(kbch, rng):
+    """(frame, expected data-field bytes) pairs of the reference's parser
+    tests (lib/qa_bbframe_parser.cc:47-139): a valid field, the largest legal
+    DFL, an empty field, every single-bit header error, DFL one byte too large,
+    DFL not a byte multiple, TS/GS other than generic packetized."""
+    cases = []
+    data = rng.integers(0, 256, 100, dtype=np.uint8)
+    cases.append((bbframe(kbch, 800, payload=data, rng=rng), 100))
+    cases.append((bbframe(kbch, 8 * kbch - 80, rng=rng), kbch - 10))
+    cases.append((bbframe(kbch, 0, rng=rng), 0))
+    for bit in range(80):
+        f = bbframe(kbch, 800, rng=rng)
+        f[bit // 8] ^= 0x80 >> (bit % 8)
+        cases.append((f, 0))
+    cases.append((bbframe(kbch, 8 * kbch - 80 + 8, rng=rng), 0))
+    cases.append((bbframe(kbch, 803, rng=rng), 0))
+    for ts in (1, 2, 3):
+        cases.append((bbframe(kbch, 800, ts_gs=ts, rng=rng), 0))
+    return cases
+
+
+@pytest.mark.parametrize("fs,rate", [(NORMAL, E.RATE_1_2), (SHORT, E.RATE_1_2)])
+def test_parser_rejections_known_answers(fs, rate):
+    import cusat_gb300 as cs
+    kbch = cs.code_info(fs, rate)["k_bch"] // 8
+    cases = header_cases(kbch, np.random.default_rng(2))
+    hard = np.stack([c[0] for c in cases])
+    want = np.array([c[1] for c in cases])
+    ones = np.ones(len(cases), np.int32)
+    out, lengths, _ = O.bb_extract(hard, kbch, ones * 5, ones, len(cases) * kbch)
+    assert (lengths == want).all()
+    # the valid field comes back descrambled, byte for byte
+    plain = cases[0][0] ^ O.bb_prbs(kbch)
+    assert (out[:100] == plain[10:110]).all()
+
+
+def test_frame_acceptance_rule():
+    # lib/qa_rx_fec_chain.cc:9-17: usable iff LDPC converged and BCH valid
+    import cusat_gb300 as cs
+    ok = cs.rx_fec_chain.frame_passes_fec_checks
+    assert ok(25, True) and ok(0, True)
+    assert not ok(-1, True) and not ok(3, False) and not ok(-1, False)
