@@ -52,7 +52,7 @@ WORKLOAD_SHORT = {"name": "short 1/2 QPSK", "code": "s2_c4", "mod_name": "QPSK",
 N_BUFS = 4          # input batches cycled through (at least; more when a batch is small)
 L2_BYTES = 160e6    # cycled inputs exceed this (GB300 L2: 129 MB)
 PIPE = 2            # chains (streams) whose consecutive batches overlap, at least
-RESIDENT_CTAS = 304 # resident decoder CTAs on a GB300 (152 SMs x 2 for short frames)
+RESIDENT_CTAS = 456 # resident decoder CTAs on a GB300 (152 SMs x 3 for short QPSK 1/2 frames)
 
 
 def n_bufs_for(wl):

@@ -535,8 +535,13 @@ __device__ void load_code(const DecodeArgs& a, unsigned char* smem, const DevCod
         s_items[k] = gc.items[k];
 }
 
+// Resident CTAs per SM the register budget is cut for: a two-lane CTA holds
+// a normal frame (one per SM); one-lane CTAs of narrow rows (short frames)
+// fit three per SM in 55 registers without spilling, wider rows two.
+constexpr int min_ctas_per_sm(int cmax, int lanes) { return lanes == 2 ? 1 : (cmax <= 5 ? 3 : 2); }
+
 template <int CMAX, int LANES>
-__global__ void __launch_bounds__(LANES * lane_threads(LANES), LANES == 2 ? 1 : 2) ldpc_layered_kernel(DecodeArgs a)
+__global__ void __launch_bounds__(LANES * lane_threads(LANES), min_ctas_per_sm(CMAX, LANES)) ldpc_layered_kernel(DecodeArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     int16_t* app = reinterpret_cast<int16_t*>(smem);
