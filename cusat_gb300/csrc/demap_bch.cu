@@ -88,17 +88,17 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
     for (int j0 = blockIdx.x * per_block + threadIdx.x; j0 - (int)threadIdx.x < d.interleaved_len;
          j0 += gridDim.x * per_block) {
         switch (sel) {
-        case 0: demap_span<0, 0, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-        case 16: demap_span<1, 0, kDemapSpan, false>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        case 0: demap_span<0, 0, kDemapSpan>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+        case 16: demap_span<1, 0, kDemapSpan>(d, pts, fr.sym, fr.out, j0, kDemapThreads, fr.noise_var, fr.llr_gain); break;
         default:
             // log-MAP: one symbol at a time (compute-bound)
             for (int u = 0; u < kDemapSpan; u++) {
                 const int j = j0 + u * kDemapThreads;
                 switch (sel) {
-                case 36: demap_span<2, 4, 1, false>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                case 37: demap_span<2, 5, 1, false>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                case 38: demap_span<2, 6, 1, false>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                default: demap_span<2, 0, 1, false>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+                case 36: demap_span<2, 4, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+                case 37: demap_span<2, 5, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+                case 38: demap_span<2, 6, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+                default: demap_span<2, 0, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 }
             }
             break;

@@ -119,9 +119,8 @@ __device__ __forceinline__ void demap_8psk(const DevDemap& d, float re, float im
 
 // APSK: log-MAP over the points (pts in shared memory), NM bits per symbol
 // (0: d.n_mod at run time; a compile-time NM resolves every label-bit test
-// and bit loop, same arithmetic).  UNROLL: point loops unrolled by 16 (one
-// MODCOD per kernel; a kernel that switches between MODCODs stays compact).
-template <int NM, bool UNROLL>
+// and bit loop, same arithmetic; the point loops are then unrolled by 16).
+template <int NM>
 __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pts, float re, float im, int j,
                                              float llr_gain, int16_t* out)
 {
@@ -138,7 +137,7 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
         s0[b] = 0.0f;
         s1[b] = 0.0f;
     }
-#pragma unroll (NM && UNROLL ? 16 : 1)
+#pragma unroll (NM ? 16 : 1)
     for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
@@ -155,7 +154,7 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
         }
     }
     const float scale = __fmul_rn(llr_gain, 0.25f);
-#pragma unroll (NM && UNROLL ? 16 : 1)
+#pragma unroll (NM ? 16 : 1)
     for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
@@ -189,7 +188,7 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
 // Demaps the symbols j0, j0 + step, ... (U of them, those inside the frame)
 // of one frame: all U loads first (memory parallelism for the formula
 // kinds), then each symbol.  KIND 0 QPSK, 1 8PSK, 2 log-MAP with NM bits.
-template <int KIND, int NM, int U, bool UNROLL = true>
+template <int KIND, int NM, int U>
 __device__ __forceinline__ void demap_span(const DevDemap& d, const float2* pts, const float2* sym, int16_t* out,
                                            int j0, int step, float noise_var, float llr_gain)
 {
@@ -209,7 +208,7 @@ __device__ __forceinline__ void demap_span(const DevDemap& d, const float2* pts,
         else if (KIND == 1)
             demap_8psk(d, s[u].x, s[u].y, j, llr_gain, out);
         else
-            demap_logmap<NM, UNROLL>(d, pts, s[u].x, s[u].y, j, llr_gain, out);
+            demap_logmap<NM>(d, pts, s[u].x, s[u].y, j, llr_gain, out);
     }
 }
 
