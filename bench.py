@@ -78,6 +78,8 @@ def parse():
                          "learned (max 20 it) min-sum on normal QPSK 1/3 at its threshold")
     ap.add_argument("--rates", default="0.5,1,2,3,4,5", help="serve: aggregate Gsym/s to sweep")
     ap.add_argument("--duration", type=float, default=0.25, help="serve: seconds of traffic per rate")
+    ap.add_argument("--pipe", type=int, default=0,
+                    help="single/short: chains whose consecutive batches overlap (0 = enough to fill the resident CTA slots, at least 2)")
     ap.add_argument("--learned", action="store_true",
                     help="mixed/serve: decode each MODCOD with its adopted learned weights where one exists")
     return ap.parse_args()
@@ -254,7 +256,7 @@ def main():
     # finish one batch's last frames start on the next batch
     # enough chains in flight that small batches (64 short frames) fill the
     # resident CTA slots
-    pipe = min(8, max(PIPE, -(-RESIDENT_CTAS // B)))
+    pipe = args.pipe or min(8, max(PIPE, -(-RESIDENT_CTAS // B)))
     rxs = [cs.rx_fec(wl["mod"], wl["rate"], wl["fs"], T, B) for _ in range(pipe)]
     streams = [torch.cuda.Stream() for _ in range(pipe)]
     d_sym = [torch.from_numpy(b).cuda() for b in bufs]
@@ -382,6 +384,10 @@ def main():
     except (OSError, KeyError, ValueError):
         pass
     edge_iters = float(np.mean(it)) * ci["edges"] * B
+    issue_frac = None
+    if prof.get("warp_instructions") and clk.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+        issue_frac = prof["warp_instructions"] / (dec_ms * 1e-3) / (sms * 4 * clk["sm_mhz"] * 1e6)
     threads = os.cpu_count() or 1
     cpu_s, n_cpu = cpu_sample(wl, bufs, n0, gain, threads, args.cpu_seconds)
     cpu_value = n_cpu * ci["k_ldpc"] / cpu_s / 1e9
@@ -417,6 +423,10 @@ def main():
                          "chain": {"launch_ms": launch_ms, "algorithmic_bytes": per_launch_bytes,
                                    "achieved_gbs": per_launch_bytes / launch_s / 1e9}}},
         "onchip": {"edge_iterations_per_s": edge_iters / (dec_ms * 1e-3),
+                   "issue_frac": issue_frac,
+                   "issue_note": "warp instructions of one decoder launch (ncu capture in profiles/) over its "
+                                 "live launch time, divided by the issue peak (SMs x 4 schedulers x median "
+                                 "SM clock): the decoder's binding roofline",
                    "alu_pipe_pct_ncu": prof.get("alu_pipe_pct"), "issue_active_pct_ncu": prof.get("issue_active_pct"),
                    "smem_app_bytes_per_s": 4.0 * edge_iters / (dec_ms * 1e-3),
                    "note": "mean iterations x Tanner edges x frames per launch; 4 B of shared-memory APP "
