@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=0, help="frames in the CPU sample (0 = auto)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall time of the CPU baseline sample")
-    ap.add_argument("--workload", choices=["single", "short", "mixed", "serve", "learned", "codes", "chain"],
+    ap.add_argument("--workload", choices=["single", "short", "mixed", "serve", "learned", "codes", "chain", "acm"],
                     default="single",
                     help="single: the headline 8PSK 3/5 batch; short: 64 short QPSK 1/2 frames; mixed: 1024 frames of 10 MODCODs in a CUDA graph; "
                          "serve: Poisson arrivals through the serving loop; learned: plain (max 50 it) vs "
@@ -241,9 +241,9 @@ def main():
     import cusat_gb300 as cs
     from cusat_gb300 import build as lib_build
     lib_build.build()
-    if args.workload in ("mixed", "serve", "learned", "codes", "chain"):
+    if args.workload in ("mixed", "serve", "learned", "codes", "chain", "acm"):
         {"mixed": mixed_main, "serve": serve_main, "learned": learned_main, "codes": codes_main,
-         "chain": chain_main}[args.workload](
+         "chain": chain_main, "acm": acm_main}[args.workload](
             args, torch, cs, rank, local_rank, world)
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -937,6 +937,62 @@ def chain_main(args, torch, cs, rank, local_rank, world):
                    "e2e_note": "host symbols in, per-frame verdicts and GSE data fields out (pinned)",
                    "host_frame_copy_us": copy_us, "host_ctypes_call_us": call_us},
         "clocks": clk}), flush=True)
+
+
+def acm_main(args, torch, cs, rank, local_rank, world):
+    """The receive pool under ACM traffic: the 10-MODCOD mix in normal
+    frames at threshold + 0.5 dB, submitted one by one from host memory with
+    the MODCOD drawn per frame (rx_fec_pool::submit), through the per-MODCOD
+    pool (the reference's design: one chain per MODCOD, wait at every MODCOD
+    change) and the mixed pool (one slot ring, multi-MODCOD launches).  Wall
+    time from the first submit to the end of finish_all_pending; value = the
+    mixed pool's info Gbit/s."""
+    from cusat_gb300 import traffic
+    from cusat_gb300.enums import find_modcod
+    table, frames = traffic.mixed_traffic(512, 2031, short_share=0.0)
+    idx = [find_modcod(name)[0] for name, _, _, _ in table]
+    kbits = [cs.code_info(fs, rate)["k_ldpc"] for _, _, rate, fs in table]
+    thr = [find_modcod(name)[5] + 0.5 for name, _, _, _ in table]
+    rows = {}
+
+    def run(pool, n):
+        pool.warmup_all()
+        for m, t in zip(idx, thr):
+            pool.update_snr(m, t)
+        bits = 0
+        t0 = time.perf_counter()
+        for f in frames[:n]:
+            if pool.submit(f["sym"], idx[f["modcod"]]):
+                while pool.get_gse_output().size:
+                    pass
+            bits += kbits[f["modcod"]]
+        pool.finish_all_pending()
+        dt = time.perf_counter() - t0
+        return {"frames": n, "gbit_s": bits / dt / 1e9, "ms": dt * 1e3, "frame_errors": pool.total_error_count()}
+
+    clocks = Clocks(local_rank)
+    clocks.start()
+    per = cs.rx_fec_pool(0, idx, 50, 64, 8, 4)
+    rows["per-MODCOD pool (reference design), micro-batch 4, 8 streams"] = run(per, 128)
+    per.close()
+    for sf in (32, 64, 128):
+        mix = cs.rx_fec_pool(0, idx, 50, 64, 4, 4, mixed=True, slot_frames=sf)
+        run(mix, 64)  # warm-up
+        rows[f"mixed pool, {sf}-frame slots, 4 streams"] = run(mix, len(frames))
+        mix.close()
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    best = max((v for k, v in rows.items() if k.startswith("mixed")), key=lambda r: r["gbit_s"])
+    changes = sum(1 for a, b in zip(frames, frames[1:]) if a["modcod"] != b["modcod"])
+    print(json.dumps({
+        "metric": METRIC, "value": best["gbit_s"], "unit": "Gbit/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": best["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int16", "data": "synthetic (seeded 10-MODCOD normal-frame ACM sequence at threshold + 0.5 dB, "
+                                  "host memory)",
+        "config": {"workload": f"rx_fec_pool under ACM: {len(frames)} frames, MODCOD changes at {changes} of "
+                               f"{len(frames) - 1} frame boundaries, submitted one by one, max 50 iterations",
+                   "pools": rows}, "clocks": clk}), flush=True)
 
 
 if __name__ == "__main__":

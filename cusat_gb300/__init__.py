@@ -710,10 +710,12 @@ class rx_fec_chain:
 
 class rx_fec_pool:
     """One rx_fec_chain per enabled MODCOD (modcod_idx values of the MODCOD
-    table) behind one decode budget; output blocks in submission order."""
+    table) behind one decode budget; output blocks in submission order.
+    mixed=True: every MODCOD in one slot ring of slot_frames-frame
+    multi-MODCOD launches, no wait at a MODCOD change, same output."""
 
     def __init__(self, framesize, enabled_modcods, max_trials=25, cuda_max_batch=64, n_gpu_streams=8,
-                 micro_batch=4):
+                 micro_batch=4, mixed=False, slot_frames=64):
         from .enums import modcod_by_index
         triples = []
         for idx in enabled_modcods:
@@ -721,9 +723,16 @@ class rx_fec_pool:
             triples += [m[0], m[1], m[2]]
         arr = np.asarray(triples, np.int32)
         h = ctypes.c_void_p()
-        _capi.check(_capi.lib().cusat_rx_pool_create(framesize, arr.ctypes.data, len(enabled_modcods), max_trials,
-                                                     cuda_max_batch, n_gpu_streams, micro_batch, ctypes.byref(h)))
+        if mixed:
+            _capi.check(_capi.lib().cusat_rx_pool_create_mixed(framesize, arr.ctypes.data, len(enabled_modcods),
+                                                               max_trials, n_gpu_streams, micro_batch, slot_frames,
+                                                               ctypes.byref(h)))
+        else:
+            _capi.check(_capi.lib().cusat_rx_pool_create(framesize, arr.ctypes.data, len(enabled_modcods),
+                                                         max_trials, cuda_max_batch, n_gpu_streams, micro_batch,
+                                                         ctypes.byref(h)))
         self._h = h
+        self.mixed = bool(mixed)
         self.modcods = [int(i) for i in enabled_modcods]
 
     def close(self):

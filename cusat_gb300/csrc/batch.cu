@@ -293,7 +293,8 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
         cudaError_t e = allow_full_smem(c.fn);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sm, c.fn, c.threads, c.proto.sm_total);
-        c.grid_max = c.per_sm * b->sms;
+        // no launch runs more CTAs than frames: message scratch for at most max_frames
+        c.grid_max = std::min(c.per_sm * b->sms, max_frames);
         if (e == cudaSuccess)
             e = cudaMalloc(&c.d_codes, codes.size() * sizeof(cusat::DevCode));
         if (e == cudaSuccess)

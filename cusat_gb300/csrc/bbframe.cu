@@ -29,13 +29,16 @@ __device__ __forceinline__ uint8_t crc8_bb(const uint8_t* d, int n)
 
 // One thread per frame: the data-field length the frame contributes (0 when
 // it is dropped): converged, BCH valid, header CRC zero, DFL <= 8 kbch - 80
-// and a multiple of 8, TS/GS generic packetized.
-__global__ void bb_header_kernel(const uint8_t* __restrict__ hard, int stride, int kbch,
-                                 const int32_t* __restrict__ trials, const int32_t* __restrict__ valid,
-                                 const uint8_t* __restrict__ prbs, int batch, int32_t* __restrict__ lengths)
+// and a multiple of 8, TS/GS generic packetized.  kbch_f: per-frame K_bch/8
+// (frames of different codes), or nullptr for kbch everywhere.
+__global__ void bb_header_kernel(const uint8_t* __restrict__ hard, int stride, int kbch_all,
+                                 const int32_t* __restrict__ kbch_f, const int32_t* __restrict__ trials,
+                                 const int32_t* __restrict__ valid, const uint8_t* __restrict__ prbs, int batch,
+                                 int32_t* __restrict__ lengths)
 {
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < batch; f += gridDim.x * blockDim.x) {
         int n = 0;
+        const int kbch = kbch_f ? kbch_f[f] : kbch_all;
         if (trials[f] >= 0 && valid[f]) {
             uint8_t h[kHeaderBytes];
             const uint8_t* src = hard + (size_t)f * stride;
@@ -88,8 +91,27 @@ __global__ void bb_copy_kernel(const uint8_t* __restrict__ hard, int stride, con
 
 struct cusat_bb_extractor {
     int kbch = 0, sms = 0;
-    uint8_t* prbs = nullptr;
+    uint8_t* prbs = nullptr;  // the scrambler sequence, kbch bytes (a prefix serves shorter codes)
 };
+
+namespace {
+
+int extract(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_stride, const int32_t* kbch_dev,
+            const int32_t* trials_dev, const int32_t* bch_valid_dev, int batch, uint8_t* out_dev, int max_out,
+            int32_t* lengths_dev, int32_t* offsets_dev, cudaStream_t s)
+{
+    bb_header_kernel<<<(batch + 255) / 256, 256, 0, s>>>(hard_dev, hard_stride, x->kbch, kbch_dev, trials_dev,
+                                                         bch_valid_dev, x->prbs, batch, lengths_dev);
+    CU(cudaGetLastError(), "BBHEADER launch");
+    bb_place_kernel<<<1, 32, 0, s>>>(batch, max_out, lengths_dev, offsets_dev);
+    CU(cudaGetLastError(), "placement launch");
+    bb_copy_kernel<<<std::min(batch, std::max(x->sms, 1) * 8), 256, 0, s>>>(hard_dev, hard_stride, x->prbs, batch,
+                                                                         lengths_dev, offsets_dev, out_dev);
+    CU(cudaGetLastError(), "data-field launch");
+    return CUSAT_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -154,16 +176,20 @@ int cusat_bb_extract(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_st
     if (!x || !hard_dev || !trials_dev || !bch_valid_dev || !lengths_dev || !offsets_dev || batch <= 0 ||
         hard_stride < x->kbch || max_out < 0 || (max_out > 0 && !out_dev))
         return fail(CUSAT_ERR_ARG, "invalid extraction arguments");
-    cudaStream_t s = (cudaStream_t)stream;
-    bb_header_kernel<<<(batch + 255) / 256, 256, 0, s>>>(hard_dev, hard_stride, x->kbch, trials_dev, bch_valid_dev,
-                                                         x->prbs, batch, lengths_dev);
-    CU(cudaGetLastError(), "BBHEADER launch");
-    bb_place_kernel<<<1, 32, 0, s>>>(batch, max_out, lengths_dev, offsets_dev);
-    CU(cudaGetLastError(), "placement launch");
-    bb_copy_kernel<<<std::min(batch, std::max(x->sms, 1) * 8), 256, 0, s>>>(hard_dev, hard_stride, x->prbs, batch,
-                                                                         lengths_dev, offsets_dev, out_dev);
-    CU(cudaGetLastError(), "data-field launch");
-    return CUSAT_OK;
+    return extract(x, hard_dev, hard_stride, nullptr, trials_dev, bch_valid_dev, batch, out_dev, max_out, lengths_dev,
+                   offsets_dev, (cudaStream_t)stream);
+}
+
+int cusat_bb_extract_frames(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_stride, const int32_t* kbch_dev,
+                            const int32_t* trials_dev, const int32_t* bch_valid_dev, int batch, uint8_t* out_dev,
+                            int max_out, int32_t* lengths_dev, int32_t* offsets_dev, void* stream)
+{
+    if (!x || !hard_dev || !kbch_dev || !trials_dev || !bch_valid_dev || !lengths_dev || !offsets_dev || batch <= 0 ||
+        max_out < 0 || (max_out > 0 && !out_dev))
+        return fail(CUSAT_ERR_ARG, "invalid extraction arguments");
+    // every frame's kbch_dev[f] must be <= the extractor's code's and <= hard_stride
+    return extract(x, hard_dev, hard_stride, kbch_dev, trials_dev, bch_valid_dev, batch, out_dev, max_out, lengths_dev,
+                   offsets_dev, (cudaStream_t)stream);
 }
 
 }  // extern "C"

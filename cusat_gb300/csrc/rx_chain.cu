@@ -717,7 +717,79 @@ struct Block {
 
 }  // namespace
 
+// Mixed pool: one slot ring for every MODCOD, each slot one multi-MODCOD
+// launch (cusat_batch) -- no flush at a MODCOD change.  The reference's
+// per-MODCOD micro-batches survive as "virtual" ones: they decide when a
+// frame's LLR gain is fixed (the MODCOD's gain when its micro-batch closes:
+// full, MODCOD change, stale, flush), which is the gain the reference's chain
+// launches it with; a slot launches once all its frames' gains are fixed.
+namespace {
+
+struct MixModcod {
+    int idx = 0, mod = 0, rate = 0;
+    int xfec = 0, k_bytes = 0, kbch_bytes = 0, bits_per_sym = 0;
+    std::vector<float> pts;
+    float snr_db = 0.0f, pilot_snr_db = 0.0f, noise_var = 1.0f, llr_gain = 4.0f;
+    int snr_skip = 0;
+    uint64_t frames = 0, errors = 0, drops = 0;
+};
+
+struct MixSlot {
+    float* sym = nullptr;    // pinned [slot_frames][max_xfec][2]
+    int32_t* res = nullptr;  // pinned: trials, valid, lengths, kbch [slot_frames each], offsets [slot_frames + 1]
+    uint8_t* out = nullptr;  // pinned: packed data fields
+    cudaEvent_t done = nullptr;
+    std::vector<int> modcod;  // per frame: index into MixPool::mc
+    std::vector<float> noise_var, llr_gain;
+    int n_frames = 0, open = 0;  // frames; frames whose gain is not fixed yet
+    bool in_flight = false;
+};
+
+struct MixLane {
+    cusat_batch* batch = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;  // the lane's last launch (its batch staging is reusable after it)
+    bool used = false;
+    float* sym_dev = nullptr;
+    uint8_t* hard_dev = nullptr;
+    std::vector<cusat_frame> frames;
+};
+
+struct MixPool {
+    std::vector<MixModcod> mc;
+    int slot_frames = 0, micro_batch = 0, max_xfec = 0, max_kbytes = 0, max_kbch = 0;
+    cusat_bb_extractor* bb = nullptr;
+    std::vector<MixSlot> flight;
+    std::vector<MixLane> lanes;
+    int submit_idx = 0, launch_idx = 0, drain_idx = 0, next_lane = 0, fill = 0;
+    int open_mc = -1;                          // MODCOD of the open virtual micro-batch
+    std::vector<std::pair<int, int>> open_at;  // its frames: (slot submit index, frame)
+    Clock::time_point open_start{};
+    std::shared_ptr<BudgetState> budget;
+    void (*lock_fn)(void*) = nullptr;
+    void (*unlock_fn)(void*) = nullptr;
+    void* lock_ctx = nullptr;
+    int failed = 0;
+
+    MixSlot& slot(int i) { return flight[i % kFlight]; }
+    int32_t* trials(MixSlot& t) const { return t.res; }
+    int32_t* valid(MixSlot& t) const { return t.res + slot_frames; }
+    int32_t* lengths(MixSlot& t) const { return t.res + 2 * slot_frames; }
+    int32_t* kbch(MixSlot& t) const { return t.res + 3 * slot_frames; }
+    int32_t* offsets(MixSlot& t) const { return t.res + 4 * slot_frames; }
+    int find(int modcod) const
+    {
+        for (size_t i = 0; i < mc.size(); i++)
+            if (mc[i].idx == modcod)
+                return (int)i;
+        return -1;
+    }
+};
+
+}  // namespace
+
 struct cusat_rx_pool {
+    std::unique_ptr<MixPool> mix;   // mixed mode, else one chain per MODCOD
     std::vector<PoolEntry> chains;  // creation order: drains and flushes visit them in it
     int last_decoded = 0, last_submitted = 0;
     bool has_prev = false;
@@ -773,6 +845,446 @@ void clear_ready(cusat_rx_pool* p)
     p->last_sizes.clear();
 }
 
+
+// ---- mixed pool ----
+
+int mix_fail(MixPool& x, int rc)
+{
+    if (!x.failed)
+        x.failed = rc;
+    return rc;
+}
+
+// Fixes the gain of the open virtual micro-batch's frames: its MODCOD's
+// current N0 and gain (what the reference's chain launches it with).
+void mix_close(MixPool& x)
+{
+    if (x.open_mc >= 0) {
+        const MixModcod& m = x.mc[x.open_mc];
+        for (const auto& at : x.open_at) {
+            MixSlot& t = x.slot(at.first);
+            t.noise_var[at.second] = m.noise_var;
+            t.llr_gain[at.second] = m.llr_gain;
+            t.open--;
+        }
+    }
+    x.open_at.clear();
+    x.open_mc = -1;
+}
+
+void mix_estimate_snr(MixModcod& m, const float* sym, int n_sym)
+{
+    float lin;
+    if (m.bits_per_sym >= 7 && m.pilot_snr_db > 5.0f)
+        lin = std::pow(10.0f, m.pilot_snr_db / 10.0f);
+    else if (m.mod == 0)
+        lin = cusat::dd_snr_qpsk(sym, n_sym);
+    else
+        lin = cusat::dd_snr_points(m.pts, sym, n_sym, 8);
+    if (lin > 1.0f) {
+        m.snr_db = 10.0f * std::log10(lin);
+        m.noise_var = 1.0f / lin;
+        m.llr_gain = std::min(4.0f / m.noise_var, 1000.0f);
+    }
+}
+
+// One slot: symbols up, the multi-MODCOD launch (demap -> per-class
+// decoders -> BCH), the per-frame-code BB stage into the slot's pinned
+// memory, completion event.
+int mix_launch(MixPool& x, MixSlot& t)
+{
+    const int li = x.next_lane++ % (int)x.lanes.size();
+    MixLane& L = x.lanes[li];
+    const int n = t.n_frames;
+    if (x.lock_fn)
+        x.lock_fn(x.lock_ctx);
+    int rc = CUSAT_OK;
+    cudaError_t e = cudaSuccess;
+    if (L.used)
+        e = cudaEventSynchronize(L.done);  // the lane's batch descriptors are staged again below
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(L.sym_dev, t.sym, (size_t)n * x.max_xfec * 2 * sizeof(float), cudaMemcpyHostToDevice,
+                            L.stream);
+    if (e != cudaSuccess)
+        rc = cuda_fail(e, "symbol copy");
+    for (int k = 0; rc == CUSAT_OK && k < n; k++) {
+        const MixModcod& m = x.mc[t.modcod[k]];
+        x.kbch(t)[k] = m.kbch_bytes;
+        cusat_frame& f = L.frames[k];
+        f.modcod = t.modcod[k];
+        f.noise_var = t.noise_var[k];
+        f.llr_gain = t.llr_gain[k];
+        f.reserved = 0;
+        f.sym = L.sym_dev + (size_t)k * x.max_xfec * 2;
+        f.hard = L.hard_dev + (size_t)k * x.max_kbytes;
+        f.trials = x.trials(t) + k;
+        f.bch_valid = x.valid(t) + k;
+    }
+    if (rc == CUSAT_OK)
+        rc = batch_launch_ready(L.batch, L.frames.data(), n, L.stream);
+    if (rc == CUSAT_OK)
+        rc = cusat_bb_extract_frames(x.bb, L.hard_dev, x.max_kbytes, x.kbch(t), x.trials(t), x.valid(t), n, t.out,
+                                     n * x.max_kbch, x.lengths(t), x.offsets(t), L.stream);
+    if (rc == CUSAT_OK) {
+        e = cudaEventRecord(t.done, L.stream);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(L.done, L.stream);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "event record");
+    }
+    if (x.unlock_fn)
+        x.unlock_fn(x.lock_ctx);
+    if (rc)
+        return mix_fail(x, rc);
+    L.used = true;
+    t.in_flight = true;
+    return CUSAT_OK;
+}
+
+// Launches ready slots in order: full (or flushed), every gain fixed, and
+// within the in-flight budget (an empty GPU always admits one).
+int mix_pump(MixPool& x, bool bypass_cap)
+{
+    while (x.launch_idx < x.submit_idx) {
+        MixSlot& t = x.slot(x.launch_idx);
+        if (t.open > 0)
+            break;
+        BudgetState* b = x.budget.get();
+        if (!bypass_cap && b && b->cap > 0) {
+            const int cur = b->in_flight.load(std::memory_order_relaxed);
+            if (cur > 0 && cur + t.n_frames > b->cap)
+                break;
+        }
+        if (b)
+            b->in_flight.fetch_add(t.n_frames, std::memory_order_relaxed);
+        const int rc = mix_launch(x, t);
+        if (rc) {
+            if (b)
+                b->in_flight.fetch_sub(t.n_frames, std::memory_order_relaxed);
+            return rc;
+        }
+        x.launch_idx++;
+    }
+    return CUSAT_OK;
+}
+
+// Counts a completed slot's frames per MODCOD and moves its output into the
+// FIFO as one block per run of same-MODCOD frames (a block belongs to one
+// MODCOD, as the reference pool's blocks do).
+void mix_retire(cusat_rx_pool* p, MixSlot& t)
+{
+    MixPool& x = *p->mix;
+    const int n = t.n_frames;
+    const int32_t* tr = x.trials(t);
+    const int32_t* va = x.valid(t);
+    const int32_t* len = x.lengths(t);
+    const int32_t* off = x.offsets(t);
+    for (int k0 = 0; k0 < n;) {
+        int k1 = k0;
+        while (k1 < n && t.modcod[k1] == t.modcod[k0])
+            k1++;
+        MixModcod& m = x.mc[t.modcod[k0]];
+        Block b;
+        if (!p->spare.empty()) {
+            b = std::move(p->spare.back());
+            p->spare.pop_back();
+        }
+        b.bytes.clear();
+        b.dfl.clear();
+        for (int k = k0; k < k1; k++) {
+            m.frames++;
+            if (!(tr[k] >= 0 && va[k])) {
+                m.errors++;
+                continue;
+            }
+            if (len[k] > 0)
+                b.dfl.push_back(len[k]);
+        }
+        const int bytes = off[k1] - off[k0];
+        if (bytes > 0) {
+            b.bytes.assign(t.out + off[k0], t.out + off[k1]);
+            b.modcod = m.idx;
+            p->last_decoded = m.idx;
+            p->ready.push_back(std::move(b));
+        } else {
+            p->spare.push_back(std::move(b));
+        }
+        k0 = k1;
+    }
+    t.in_flight = false;
+    if (x.budget)
+        x.budget->in_flight.fetch_sub(n, std::memory_order_relaxed);
+    x.drain_idx++;
+}
+
+int mix_drain(cusat_rx_pool* p)
+{
+    MixPool& x = *p->mix;
+    while (x.drain_idx < x.launch_idx) {
+        MixSlot& t = x.slot(x.drain_idx);
+        if (!t.in_flight) {
+            x.drain_idx++;
+            continue;
+        }
+        const cudaError_t e = cudaEventQuery(t.done);
+        if (e == cudaErrorNotReady)
+            break;
+        if (e != cudaSuccess)
+            return mix_fail(x, cuda_fail(e, "decode slot"));
+        mix_retire(p, t);
+    }
+    return mix_pump(x, false);
+}
+
+// Closes the open micro-batch and submits the partial slot.
+void mix_seal(MixPool& x)
+{
+    mix_close(x);
+    if (x.fill > 0) {
+        x.submit_idx++;
+        x.fill = 0;
+    }
+}
+
+int mix_finish(cusat_rx_pool* p)
+{
+    MixPool& x = *p->mix;
+    mix_seal(x);
+    int rc = mix_pump(x, true);
+    while (rc == CUSAT_OK && x.drain_idx < x.submit_idx) {
+        if (x.drain_idx >= x.launch_idx) {
+            rc = mix_pump(x, true);
+            if (rc)
+                break;
+        }
+        MixSlot& t = x.slot(x.drain_idx);
+        if (!t.in_flight) {
+            x.drain_idx++;
+            continue;
+        }
+        const cudaError_t e = cudaEventSynchronize(t.done);
+        if (e != cudaSuccess)
+            return mix_fail(x, cuda_fail(e, "decode slot"));
+        mix_retire(p, t);
+    }
+    return rc;
+}
+
+// rx_fec_pool::submit for the mixed pool (rx_fec_pool.cc:48-87 semantics:
+// frames in submission order; the flush at a MODCOD change becomes the close
+// of that MODCOD's micro-batch, without waiting).
+int mix_submit(cusat_rx_pool* p, const float* symbols, int n_symbols, int modcod)
+{
+    MixPool& x = *p->mix;
+    const int mi = x.find(modcod);
+    if (mi < 0)
+        return 0;  // MODCOD not enabled: skipped
+    if (x.failed)
+        return x.failed;
+    if (x.fill == 0 || x.submit_idx - x.drain_idx >= kFlight / 2) {
+        const int rc = mix_drain(p);
+        if (rc)
+            return rc;
+    }
+    MixModcod& m = x.mc[mi];
+    if (x.submit_idx - x.drain_idx >= kFlight - 2 || n_symbols != m.xfec) {
+        m.drops++;
+        m.frames++;
+        m.errors++;
+        return p->ready.empty() ? 0 : 1;
+    }
+    if (x.open_mc >= 0 && x.open_mc != mi)
+        mix_close(x);
+    MixSlot& t = x.slot(x.submit_idx);
+    const int k = x.fill;
+    float* dest = t.sym + (size_t)k * x.max_xfec * 2;
+    memcpy(dest, symbols, (size_t)n_symbols * 2 * sizeof(float));
+    if (++m.snr_skip >= kSnrPeriod) {
+        m.snr_skip = 0;
+        mix_estimate_snr(m, dest, n_symbols);
+    }
+    t.modcod[k] = mi;
+    t.open++;
+    if (x.open_at.empty())
+        x.open_start = Clock::now();
+    x.open_mc = mi;
+    x.open_at.push_back(std::make_pair(x.submit_idx, k));
+    t.n_frames = ++x.fill;
+    if ((int)x.open_at.size() >= x.micro_batch)
+        mix_close(x);
+    if (x.fill >= x.slot_frames) {
+        x.submit_idx++;
+        x.fill = 0;
+    }
+    const int rc = mix_pump(x, false);
+    if (rc)
+        return rc;
+    return p->ready.empty() ? 0 : 1;
+}
+
+int mix_reset(cusat_rx_pool* p)
+{
+    MixPool& x = *p->mix;
+    int rc = CUSAT_OK;
+    if (x.lock_fn)
+        x.lock_fn(x.lock_ctx);
+    for (int i = x.drain_idx; i < x.submit_idx; i++) {
+        MixSlot& t = x.slot(i);
+        if (t.in_flight) {
+            const cudaError_t e = cudaEventSynchronize(t.done);
+            if (e != cudaSuccess && rc == CUSAT_OK)
+                rc = cuda_fail(e, "decode slot");
+            if (x.budget)
+                x.budget->in_flight.fetch_sub(t.n_frames, std::memory_order_relaxed);
+        }
+        t.in_flight = false;
+        t.n_frames = t.open = 0;
+    }
+    if (x.fill > 0) {
+        MixSlot& t = x.slot(x.submit_idx);
+        t.n_frames = t.open = 0;
+    }
+    if (x.unlock_fn)
+        x.unlock_fn(x.lock_ctx);
+    x.submit_idx = x.launch_idx = x.drain_idx = x.next_lane = x.fill = 0;
+    x.open_at.clear();
+    x.open_mc = -1;
+    for (MixModcod& m : x.mc) {
+        // rx_fec_chain::reset: SNR state and counters, not the drop count nor
+        // the frames-since-estimate counter
+        m.snr_db = 0.0f;
+        m.noise_var = 1.0f;
+        m.llr_gain = 4.0f;
+        m.frames = m.errors = 0;
+    }
+    return rc ? mix_fail(x, rc) : CUSAT_OK;
+}
+
+void mix_free(MixPool* x)
+{
+    if (!x)
+        return;
+    for (MixLane& L : x->lanes) {
+        if (L.stream)
+            cudaStreamSynchronize(L.stream);
+        cusat_batch_destroy(L.batch);
+        if (L.sym_dev)
+            cudaFree(L.sym_dev);
+        if (L.hard_dev)
+            cudaFree(L.hard_dev);
+        if (L.done)
+            cudaEventDestroy(L.done);
+        if (L.stream)
+            cudaStreamDestroy(L.stream);
+    }
+    for (MixSlot& t : x->flight) {
+        if (t.sym)
+            cudaFreeHost(t.sym);
+        if (t.res)
+            cudaFreeHost(t.res);
+        if (t.out)
+            cudaFreeHost(t.out);
+        if (t.done)
+            cudaEventDestroy(t.done);
+    }
+    cusat_bb_extractor_destroy(x->bb);
+    delete x;
+}
+
+int mix_create(int framesize, const int32_t* modcods, int n_modcods, int max_trials, int n_streams, int micro_batch,
+               int slot_frames, MixPool** out)
+{
+    *out = nullptr;
+    MixPool* x = new MixPool();
+    x->slot_frames = slot_frames;
+    x->micro_batch = micro_batch;
+    int rc = CUSAT_OK;
+    std::vector<int32_t> triples;
+    int longest = -1;
+    for (int i = 0; i < n_modcods && rc == CUSAT_OK; i++) {
+        MixModcod m;
+        m.idx = modcods[3 * i];
+        m.mod = modcods[3 * i + 1];
+        m.rate = modcods[3 * i + 2];
+        if (x->find(m.idx) >= 0) {
+            rc = fail(CUSAT_ERR_ARG, "MODCOD listed twice");
+            break;
+        }
+        int32_t mi[6];
+        std::vector<float> pts(512);
+        uint32_t col[8];
+        rc = cusat_modcod_info(m.mod, m.rate, framesize, pts.data(), col, mi);
+        if (rc)
+            break;
+        int32_t ci[12];
+        rc = cusat_code_info(framesize, m.rate, ci);
+        if (rc)
+            break;
+        m.xfec = mi[3];
+        m.k_bytes = ci[1] / 8;
+        m.kbch_bytes = ci[2] / 8;
+        m.bits_per_sym = cusat::make_constellation(m.mod, m.rate, framesize, &m.pts);
+        if (m.bits_per_sym <= 0) {
+            rc = fail(CUSAT_ERR_UNSUPPORTED, "constellation");
+            break;
+        }
+        x->max_xfec = std::max(x->max_xfec, m.xfec);
+        x->max_kbytes = std::max(x->max_kbytes, m.k_bytes);
+        if (m.kbch_bytes > x->max_kbch) {
+            x->max_kbch = m.kbch_bytes;
+            longest = m.rate;
+        }
+        triples.push_back(m.mod);
+        triples.push_back(m.rate);
+        triples.push_back(framesize);
+        x->mc.push_back(m);
+    }
+    if (rc == CUSAT_OK)
+        rc = cusat_bb_extractor_create(framesize, longest, &x->bb);
+    x->lanes.resize(n_streams);
+    x->flight.resize(kFlight);
+    const size_t sym_bytes = (size_t)slot_frames * x->max_xfec * 2 * sizeof(float);
+    for (MixLane& L : x->lanes) {
+        if (rc)
+            break;
+        rc = cusat_batch_create(triples.data(), n_modcods, max_trials, slot_frames, &L.batch);
+        if (rc)
+            break;
+        L.frames.resize(slot_frames);
+        cudaError_t e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&L.sym_dev, sym_bytes);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&L.hard_dev, (size_t)slot_frames * x->max_kbytes);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "mixed pool stream buffers");
+    }
+    for (size_t i = 0; rc == CUSAT_OK && i < x->flight.size(); i++) {
+        MixSlot& t = x->flight[i];
+        t.modcod.assign(slot_frames, 0);
+        t.noise_var.assign(slot_frames, 1.0f);
+        t.llr_gain.assign(slot_frames, 4.0f);
+        cudaError_t e = cudaMallocHost(&t.sym, sym_bytes);
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&t.res, (size_t)(5 * slot_frames + 1) * sizeof(int32_t));
+        if (e == cudaSuccess)
+            e = cudaMallocHost(&t.out, (size_t)slot_frames * x->max_kbch);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&t.done, cudaEventDisableTiming);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "mixed pool slot");
+    }
+    if (rc) {
+        mix_free(x);
+        return rc;
+    }
+    x->budget = default_budget();
+    *out = x;
+    return CUSAT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -813,12 +1325,44 @@ int cusat_rx_pool_create(int framesize, const int32_t* modcods, int n_modcods, i
     return CUSAT_OK;
 }
 
+int cusat_rx_pool_create_mixed(int framesize, const int32_t* modcods, int n_modcods, int max_trials,
+                               int n_gpu_streams, int micro_batch, int slot_frames, cusat_rx_pool** out)
+{
+    if (!out || !modcods || n_modcods <= 0 || n_modcods > 256 || max_trials < 0 || max_trials > 1000 ||
+        n_gpu_streams <= 0 || n_gpu_streams > 64 || micro_batch <= 0 || slot_frames <= 0 || slot_frames > 4096)
+        return fail(CUSAT_ERR_ARG, "invalid pool arguments");
+    *out = nullptr;
+    int dev;
+    int rc = require_device(&dev);
+    if (rc)
+        return rc;
+    cusat_rx_pool* p = new cusat_rx_pool();
+    MixPool* x = nullptr;
+    rc = mix_create(framesize, modcods, n_modcods, max_trials, n_gpu_streams, micro_batch, slot_frames, &x);
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    p->mix.reset(x);
+    p->budget.s = x->budget;
+    p->max_output_bytes = x->max_kbch * micro_batch * kFlight;
+    *out = p;
+    return CUSAT_OK;
+}
+
 void cusat_rx_pool_destroy(cusat_rx_pool* p)
 {
     if (!p)
         return;
     for (PoolEntry& e : p->chains)
         cusat_rx_chain_destroy(e.chain);
+    if (p->mix) {
+        MixPool* x = p->mix.release();
+        for (int i = x->drain_idx; i < x->launch_idx; i++)
+            if (x->slot(i).in_flight && x->budget)
+                x->budget->in_flight.fetch_sub(x->slot(i).n_frames, std::memory_order_relaxed);
+        mix_free(x);
+    }
     delete p;
 }
 
@@ -830,6 +1374,8 @@ int cusat_rx_pool_submit(cusat_rx_pool* p, const float* symbols, int n_symbols, 
 {
     if (!p)
         return fail(CUSAT_ERR_ARG, "null pool");
+    if (p->mix)
+        return mix_submit(p, symbols, n_symbols, modcod);
     cusat_rx_chain* c = p->find(modcod);
     if (!c)
         return 0;  // MODCOD not enabled: skipped
@@ -891,6 +1437,12 @@ int cusat_rx_pool_drain_all_completed(cusat_rx_pool* p)
 {
     if (!p)
         return fail(CUSAT_ERR_ARG, "null pool");
+    if (p->mix) {
+        if (p->mix->failed)
+            return p->mix->failed;
+        const int rc = mix_drain(p);
+        return rc ? rc : (p->ready.empty() ? 0 : 1);
+    }
     int any = 0;
     for (PoolEntry& e : p->chains) {
         const int rc = cusat_rx_chain_drain_completed(e.chain);
@@ -908,6 +1460,8 @@ int cusat_rx_pool_finish_all_pending(cusat_rx_pool* p)
 {
     if (!p)
         return fail(CUSAT_ERR_ARG, "null pool");
+    if (p->mix)
+        return p->mix->failed ? p->mix->failed : mix_finish(p);
     for (PoolEntry& e : p->chains) {
         const int rc = cusat_rx_chain_flush(e.chain);
         if (rc)
@@ -925,6 +1479,20 @@ int cusat_rx_pool_launch_stale(cusat_rx_pool* p, double max_age_ms)
         return fail(CUSAT_ERR_ARG, "null pool");
     const Clock::time_point now = Clock::now();
     int launched = 0;
+    if (p->mix) {
+        MixPool& x = *p->mix;
+        if (x.failed)
+            return x.failed;
+        if (!x.open_at.empty() &&
+            std::chrono::duration<double, std::milli>(now - x.open_start).count() >= max_age_ms) {
+            mix_seal(x);
+            const int rc = mix_pump(x, false);
+            if (rc)
+                return rc;
+            launched = 1;
+        }
+        return launched;
+    }
     for (PoolEntry& e : p->chains) {
         cusat_rx_chain* c = e.chain;
         if (c->batch_idx > 0 &&
@@ -942,7 +1510,7 @@ int cusat_rx_pool_reset_all(cusat_rx_pool* p)
 {
     if (!p)
         return fail(CUSAT_ERR_ARG, "null pool");
-    int rc = CUSAT_OK;
+    int rc = p->mix ? mix_reset(p) : CUSAT_OK;
     for (PoolEntry& e : p->chains) {
         const int r = cusat_rx_chain_reset(e.chain);
         if (r && rc == CUSAT_OK)
@@ -958,6 +1526,28 @@ int cusat_rx_pool_warmup_all(cusat_rx_pool* p)
 {
     if (!p)
         return fail(CUSAT_ERR_ARG, "null pool");
+    if (p->mix) {
+        // rx_fec_chain::warmup per MODCOD: one all-zero frame through the
+        // path, then a clean state (each MODCOD's frames-since-estimate
+        // counter keeps the one frame, as the reference's chains do)
+        MixPool& x = *p->mix;
+        std::vector<float> zeros((size_t)x.max_xfec * 2, 0.0f);
+        int rc = CUSAT_OK;
+        for (const MixModcod& m : x.mc) {
+            rc = mix_submit(p, zeros.data(), m.xfec, m.idx);
+            if (rc < 0)
+                return rc;
+        }
+        rc = mix_finish(p);
+        if (rc == CUSAT_OK)
+            rc = mix_reset(p);
+        for (MixModcod& m : x.mc)
+            m.drops = 0;
+        p->last_decoded = p->last_submitted = 0;
+        p->has_prev = false;
+        clear_ready(p);
+        return rc;
+    }
     for (PoolEntry& e : p->chains) {
         const int rc = cusat_rx_chain_warmup(e.chain);
         if (rc)
@@ -971,14 +1561,33 @@ int cusat_rx_pool_warmup_all(cusat_rx_pool* p)
 
 void cusat_rx_pool_update_snr(cusat_rx_pool* p, int modcod, float snr_db)
 {
-    if (p)
-        cusat_rx_chain_update_snr(p->find(modcod), snr_db);
+    if (!p)
+        return;
+    if (p->mix) {
+        const int mi = p->mix->find(modcod);
+        if (mi < 0 || !(snr_db > 0.0f))
+            return;
+        MixModcod& m = p->mix->mc[mi];
+        const float lin = std::pow(10.0f, snr_db / 10.0f);
+        m.pilot_snr_db = snr_db;
+        m.snr_db = snr_db;
+        m.noise_var = 1.0f / lin;
+        m.llr_gain = std::min(4.0f / m.noise_var, 1000.0f);
+        return;
+    }
+    cusat_rx_chain_update_snr(p->find(modcod), snr_db);
 }
 
 int cusat_rx_pool_set_launch_lock(cusat_rx_pool* p, void (*lock)(void*), void (*unlock)(void*), void* ctx)
 {
-    if (!p)
-        return fail(CUSAT_ERR_ARG, "null pool");
+    if (!p || (!lock) != (!unlock))
+        return fail(CUSAT_ERR_ARG, "lock and unlock go together");
+    if (p->mix) {
+        p->mix->lock_fn = lock;
+        p->mix->unlock_fn = unlock;
+        p->mix->lock_ctx = ctx;
+        return CUSAT_OK;
+    }
     for (PoolEntry& e : p->chains) {
         const int rc = cusat_rx_chain_set_launch_lock(e.chain, lock, unlock, ctx);
         if (rc)
@@ -994,6 +1603,14 @@ int cusat_rx_pool_stats(const cusat_rx_pool* p, double* out)
     if (!p || !out)
         return fail(CUSAT_ERR_ARG, "null argument");
     double f = 0, e = 0, d = 0, snr = 0;
+    if (p->mix)
+        for (const MixModcod& m : p->mix->mc) {
+            f += (double)m.frames;
+            e += (double)m.errors;
+            d += (double)m.drops;
+            if (m.idx == p->last_decoded)
+                snr = m.snr_db;
+        }
     for (const PoolEntry& c : p->chains) {
         f += (double)c.chain->frames;
         e += (double)c.chain->errors;
@@ -1013,6 +1630,14 @@ int cusat_rx_pool_modcod_counters(const cusat_rx_pool* p, int modcod, uint64_t* 
 {
     if (!p || !frames || !errors)
         return fail(CUSAT_ERR_ARG, "null argument");
+    if (p->mix) {
+        const int mi = p->mix->find(modcod);
+        if (mi < 0)
+            return 0;
+        *frames = p->mix->mc[mi].frames;
+        *errors = p->mix->mc[mi].errors;
+        return 1;
+    }
     for (const PoolEntry& c : p->chains)
         if (c.modcod == modcod) {
             *frames = c.chain->frames;

@@ -362,6 +362,12 @@ void cusat_bb_extractor_destroy(cusat_bb_extractor* x);
 int cusat_bb_extract(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_stride, const int32_t* trials_dev,
                      const int32_t* bch_valid_dev, int batch, uint8_t* out_dev, int max_out, int32_t* lengths_dev,
                      int32_t* offsets_dev, void* stream);
+/* The same over frames of different codes: kbch_dev[f] = K_bch/8 of frame f
+ * (device or mapped pinned memory), each at most the extractor's code's
+ * (create it for the longest code of the batch) and at most hard_stride. */
+int cusat_bb_extract_frames(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_stride, const int32_t* kbch_dev,
+                            const int32_t* trials_dev, const int32_t* bch_valid_dev, int batch, uint8_t* out_dev,
+                            int max_out, int32_t* lengths_dev, int32_t* offsets_dev, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* Frame-at-a-time receive chain and per-MODCOD pool                       */
@@ -436,6 +442,20 @@ int cusat_rx_chain_stats(const cusat_rx_chain* c, double* out);
 typedef struct cusat_rx_pool cusat_rx_pool;
 int cusat_rx_pool_create(int framesize, const int32_t* modcods, int n_modcods, int max_trials, int cuda_max_batch,
                          int n_gpu_streams, int micro_batch, cusat_rx_pool** out);
+/* The same pool with every MODCOD in one slot ring (no counterpart in the
+ * reference, which runs one chain per MODCOD and waits for the previous
+ * MODCOD's chain at every MODCOD change): frames of any MODCOD fill slots of
+ * slot_frames frames, each slot one multi-MODCOD launch (cusat_batch) with the
+ * BB stage per frame code, drained in submission order; no wait at a MODCOD
+ * change.  micro_batch keeps the reference's per-MODCOD micro-batches as the
+ * points where a frame's LLR gain is fixed (its MODCOD's gain when that
+ * micro-batch fills, the MODCOD changes, it goes stale or the pool is
+ * flushed: the gain the reference's chain launches it with), so the output
+ * equals the per-MODCOD pool's whenever that pool's launches are not deferred
+ * by the in-flight budget.  Output blocks hold one run of same-MODCOD frames.
+ * cusat_rx_pool_chain returns NULL for this pool. */
+int cusat_rx_pool_create_mixed(int framesize, const int32_t* modcods, int n_modcods, int max_trials,
+                               int n_gpu_streams, int micro_batch, int slot_frames, cusat_rx_pool** out);
 void cusat_rx_pool_destroy(cusat_rx_pool* p);
 /* the pool's chain of one MODCOD (owned by the pool), or NULL */
 cusat_rx_chain* cusat_rx_pool_chain(cusat_rx_pool* p, int modcod);

@@ -438,8 +438,11 @@ class rx_fec_pool
   public:
     typedef std::complex<float> sym_t;
 
+    // mixed: every MODCOD in one slot ring of slot_frames-frame launches
+    // (cusat_rx_pool_create_mixed); the reference's arguments keep their meaning
     rx_fec_pool(fecframe_size_t framesize, const std::vector<uint8_t>& enabled_modcods, int max_trials = 25,
-                int cuda_max_batch = 64, int n_gpu_streams = 8, int micro_batch = 4)
+                int cuda_max_batch = 64, int n_gpu_streams = 8, int micro_batch = 4, bool mixed = false,
+                int slot_frames = 64)
     {
         std::vector<int32_t> triples;
         for (uint8_t idx : enabled_modcods) {
@@ -450,8 +453,10 @@ class rx_fec_pool
             triples.push_back((int32_t)def->constellation);
             triples.push_back((int32_t)def->code_rate);
         }
-        const int rc = cusat_rx_pool_create((int)framesize, triples.data(), (int)enabled_modcods.size(),
-                                            max_trials, cuda_max_batch, n_gpu_streams, micro_batch, &p_);
+        const int rc = mixed ? cusat_rx_pool_create_mixed((int)framesize, triples.data(), (int)enabled_modcods.size(),
+                                                          max_trials, n_gpu_streams, micro_batch, slot_frames, &p_)
+                             : cusat_rx_pool_create((int)framesize, triples.data(), (int)enabled_modcods.size(),
+                                                    max_trials, cuda_max_batch, n_gpu_streams, micro_batch, &p_);
         if (rc)
             cusat_shim::die(rc, "rx_fec_pool");
     }

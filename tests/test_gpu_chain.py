@@ -236,3 +236,85 @@ def test_pool_output_in_submission_order(cuda):
     assert pool.submit(np.zeros(2 * pool.chain(A).xfecframe_len, np.float32), 99) is False   # not enabled
     pool.reset_all()
     assert pool.total_frame_count() == 0
+
+
+def _drain_pool(pool, out, dfl):
+    while True:
+        o = pool.get_gse_output()
+        if o.size == 0:
+            return
+        out.append(o)
+        dfl += pool.gse_dfl_sizes()
+
+
+def _run_pool(pool, seq, warm=True):
+    """Submits (frame, modcod) in order, collecting output as reported, then
+    finishes; returns (bytes, data-field sizes)."""
+    if warm:
+        pool.warmup_all()
+    out, dfl = [], []
+    for f, m in seq:
+        if pool.submit(f, m):
+            _drain_pool(pool, out, dfl)
+    pool.finish_all_pending()
+    _drain_pool(pool, out, dfl)
+    return (np.concatenate(out) if out else np.zeros(0, np.uint8)), dfl
+
+
+@pytest.mark.parametrize("pattern", ["runs", "random"])
+def test_mixed_pool_equals_per_modcod_pool(cuda, monkeypatch, pattern):
+    """The mixed pool (one slot ring, multi-MODCOD launches, no wait at a
+    MODCOD change) returns exactly the per-MODCOD pool's bytes, data-field
+    sizes and counters -- SNR re-estimates included -- when the per-MODCOD
+    pool's launches are not deferred by the in-flight cap."""
+    monkeypatch.setenv("CUSAT_LDPC_INFLIGHT_CAP", "0")
+    mods = [4, 12, 18]                                  # qpsk1/2, 8psk3/5, 16apsk2/3 (short)
+    pools = {}
+    frames = {}
+    for idx in mods:
+        mm = E.modcod_by_index(idx)
+        frames[idx] = list(traffic(mm[1], mm[2], SHORT, 44, mm[5] + 0.8, seed=100 + idx))
+    rng = np.random.default_rng(9)
+    if pattern == "runs":
+        order = [4] * 7 + [12] * 5 + [18] * 9 + [4] * 3 + [12] * 17 + [18] * 30 + [4] * 34 + [12] * 22 + [18] * 5
+    else:
+        order = list(rng.permutation([m for m in mods for _ in range(40)]))
+    used = {m: 0 for m in mods}
+    seq = []
+    for m in order:
+        seq.append((frames[m][used[m] % 44], int(m)))
+        used[m] += 1
+    per = cs.rx_fec_pool(SHORT, mods, 50, 64, 2, 4)
+    mix = cs.rx_fec_pool(SHORT, mods, 50, 64, 2, 4, mixed=True, slot_frames=16)
+    for p in (per, mix):
+        p.warmup_all()
+        for idx in mods:
+            p.update_snr(idx, E.modcod_by_index(idx)[5] + 0.8)
+    out_p, dfl_p = _run_pool(per, seq, warm=False)
+    out_m, dfl_m = _run_pool(mix, seq, warm=False)
+    assert len(dfl_p) > len(seq) // 2
+    assert out_m.size == out_p.size and (out_m == out_p).all() and dfl_m == dfl_p
+    for idx in mods:
+        assert mix.modcod_counters(idx) == per.modcod_counters(idx)
+    assert mix.total_frame_count() == per.total_frame_count() == len(seq)
+    assert mix.total_error_count() == per.total_error_count() > 0
+
+
+def test_mixed_pool_stale_launch_and_reset(cuda):
+    pool = cs.rx_fec_pool(SHORT, [4, 12], 50, 64, 2, 4, mixed=True, slot_frames=32)
+    pool.warmup_all()
+    mm = E.modcod_by_index(4)
+    pool.update_snr(4, mm[5] + 1.0)
+    fr = traffic(mm[1], mm[2], SHORT, 3, mm[5] + 1.0, seed=3)   # frame 2 is sent 4 dB lower
+    for f in fr:
+        pool.submit(f, 4)
+    assert pool.launch_stale(0.0) is True           # the open micro-batch and partial slot go
+    import time
+    for _ in range(2000):
+        if pool.drain_all_completed():
+            break
+        time.sleep(0.001)
+    assert pool.modcod_counters(4) == (3, 1)
+    assert pool.chain(4) is None
+    pool.reset_all()
+    assert pool.total_frame_count() == 0
