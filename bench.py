@@ -862,9 +862,10 @@ def codes_main(args, torch, cs, rank, local_rank, world):
                                "L2 for the short codes)", "codes": rows}}), flush=True)
 
 
-# (micro_batch, streams, decode budget: -1 = one frame per SM, 0 = unlimited);
-# (4, 8, -1) is the reference's default
-CHAIN_SETTINGS = [(4, 8, -1), (16, 8, -1), (64, 4, -1), (64, 4, 0), (128, 4, 0), (256, 2, 0)]
+# (micro_batch, streams, decode budget: -1 = one frame per SM, 0 = unlimited,
+# copy helper threads); (4, 8, -1, 0) is the reference's default
+CHAIN_SETTINGS = [(4, 8, -1, 0), (16, 8, -1, 0), (64, 4, -1, 0), (64, 4, 0, 0), (128, 4, 0, 0), (128, 4, 0, 3),
+                  (128, 4, -1, 3)]
 
 
 def chain_main(args, torch, cs, rank, local_rank, world):
@@ -881,10 +882,11 @@ def chain_main(args, torch, cs, rank, local_rank, world):
     rows = {}
     clocks = Clocks(local_rank)
     clocks.start()
-    for mb, streams, cap in CHAIN_SETTINGS:
+    for mb, streams, cap, helpers in CHAIN_SETTINGS:
         chain = cs.rx_fec_chain(wl["fs"], wl["rate"], wl["mod"], wl["max_trials"], 64, streams, mb)
         budget = cs.gpu_decode_budget(cap)
         chain.set_decode_budget(budget)
+        chain.set_copy_threads(helpers)
         chain.set_block_when_full(True)
         chain.warmup()
         chain.update_snr(wl["esn0_db"])
@@ -903,7 +905,7 @@ def chain_main(args, torch, cs, rank, local_rank, world):
             k += 1
         chain.flush()
         dt = time.perf_counter() - t0
-        rows[f"micro_batch {mb}, {streams} streams, budget {budget.cap or 'unlimited'}"] = {
+        rows[f"micro_batch {mb}, {streams} streams, budget {budget.cap or 'unlimited'}, copy helpers {helpers}"] = {
             "gbit_s": n * ci["k_ldpc"] / dt / 1e9, "ms_per_step": dt * 1e3 / args.steps,
             "frames_per_s": n / dt, "host_us_per_submit": t_submit / n * 1e6,
             "force_drains": chain.force_drain_count(), "errors": chain.frame_error_count()}
@@ -975,10 +977,11 @@ def acm_main(args, torch, cs, rank, local_rank, world):
     per = cs.rx_fec_pool(0, idx, 50, 64, 8, 4)
     rows["per-MODCOD pool (reference design), micro-batch 4, 8 streams"] = run(per, 128)
     per.close()
-    for sf in (32, 64, 128):
+    for sf, helpers in ((32, 0), (64, 0), (128, 0), (128, 3)):
         mix = cs.rx_fec_pool(0, idx, 50, 64, 4, 4, mixed=True, slot_frames=sf)
+        mix.set_copy_threads(helpers)
         run(mix, 64)  # warm-up
-        rows[f"mixed pool, {sf}-frame slots, 4 streams"] = run(mix, len(frames))
+        rows[f"mixed pool, {sf}-frame slots, 4 streams, copy helpers {helpers}"] = run(mix, len(frames))
         mix.close()
     clk = clocks.stop()
     if rank != 0:

@@ -652,6 +652,10 @@ class rx_fec_chain:
     def set_block_when_full(self, on):
         _capi.lib().cusat_rx_chain_set_block_when_full(self._h, 1 if on else 0)
 
+    def set_copy_threads(self, helpers):
+        """Split each frame's copy into the ring across `helpers` threads."""
+        _capi.check(_capi.lib().cusat_rx_chain_set_copy_threads(self._h, helpers))
+
     def set_decode_budget(self, budget):
         if budget is not None:
             _capi.check(_capi.lib().cusat_rx_chain_set_decode_budget(self._h, budget._h))
@@ -784,6 +788,9 @@ class rx_fec_pool:
 
     def update_snr(self, modcod, snr_db):
         _capi.lib().cusat_rx_pool_update_snr(self._h, modcod, snr_db)
+
+    def set_copy_threads(self, helpers):
+        _capi.check(_capi.lib().cusat_rx_pool_set_copy_threads(self._h, helpers))
 
     def _stats(self):
         out = np.zeros(5, np.float64)

@@ -114,6 +114,8 @@ _SIGS = {
     "cusat_rx_chain_set_launch_lock": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                       ctypes.c_void_p]),
     "cusat_rx_chain_set_block_when_full": (None, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_chain_set_copy_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_pool_set_copy_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cusat_rx_chain_update_snr": (None, [ctypes.c_void_p, ctypes.c_float]),
     "cusat_rx_chain_submit_xfecframe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_rx_chain_drain_completed": (ctypes.c_int, [ctypes.c_void_p]),

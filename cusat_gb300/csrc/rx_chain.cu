@@ -18,11 +18,15 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <deque>
 #include <memory>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/cusat_fec.h"
+#include "copy_crew.h"
 #include "engine.h"
 
 using namespace cusat_internal;
@@ -52,6 +56,16 @@ std::shared_ptr<BudgetState> default_budget()
     if (const char* e = getenv("CUSAT_LDPC_INFLIGHT_CAP"))
         b->cap = atoi(e);
     return b;
+}
+
+using cusat_internal::CopyCrew;
+
+void copy_frame(const std::shared_ptr<CopyCrew>& crew, void* dst, const void* src, size_t bytes)
+{
+    if (crew)
+        crew->copy(dst, src, bytes);
+    else
+        memcpy(dst, src, bytes);
 }
 
 // Pinned per-slot state; the device writes results straight into it.
@@ -99,6 +113,7 @@ struct cusat_rx_chain {
     void (*lock_fn)(void*) = nullptr;
     void (*unlock_fn)(void*) = nullptr;
     void* lock_ctx = nullptr;
+    std::shared_ptr<CopyCrew> crew;  // frame copies split across helper threads, or none
     int failed = 0;  // first CUDA failure; the chain refuses work afterwards
 
     Slot& slot(int idx) { return flight[idx % kFlight]; }
@@ -504,6 +519,14 @@ int cusat_rx_chain_set_launch_lock(cusat_rx_chain* c, void (*lock)(void*), void 
     return CUSAT_OK;
 }
 
+int cusat_rx_chain_set_copy_threads(cusat_rx_chain* c, int helpers)
+{
+    if (!c || helpers < 0 || helpers > 32)
+        return fail(CUSAT_ERR_ARG, "invalid copy thread count");
+    c->crew = helpers ? std::make_shared<CopyCrew>(helpers) : nullptr;
+    return CUSAT_OK;
+}
+
 void cusat_rx_chain_set_block_when_full(cusat_rx_chain* c, int on)
 {
     if (c)
@@ -552,7 +575,7 @@ int cusat_rx_chain_submit_xfecframe(cusat_rx_chain* c, const float* symbols, int
     }
     Slot& s = c->slot(c->submit_idx);
     float* dest = s.sym + (size_t)c->batch_idx * c->xfec * 2;
-    memcpy(dest, symbols, (size_t)n_symbols * 2 * sizeof(float));
+    copy_frame(c->crew, dest, symbols, (size_t)n_symbols * 2 * sizeof(float));
     if (++c->snr_skip >= kSnrPeriod) {
         c->snr_skip = 0;
         estimate_snr(c, dest, n_symbols);
@@ -769,6 +792,7 @@ struct MixPool {
     void (*lock_fn)(void*) = nullptr;
     void (*unlock_fn)(void*) = nullptr;
     void* lock_ctx = nullptr;
+    std::shared_ptr<CopyCrew> crew;
     int failed = 0;
 
     MixSlot& slot(int i) { return flight[i % kFlight]; }
@@ -1098,7 +1122,7 @@ int mix_submit(cusat_rx_pool* p, const float* symbols, int n_symbols, int modcod
     MixSlot& t = x.slot(x.submit_idx);
     const int k = x.fill;
     float* dest = t.sym + (size_t)k * x.max_xfec * 2;
-    memcpy(dest, symbols, (size_t)n_symbols * 2 * sizeof(float));
+    copy_frame(x.crew, dest, symbols, (size_t)n_symbols * 2 * sizeof(float));
     if (++m.snr_skip >= kSnrPeriod) {
         m.snr_skip = 0;
         mix_estimate_snr(m, dest, n_symbols);
@@ -1556,6 +1580,18 @@ int cusat_rx_pool_warmup_all(cusat_rx_pool* p)
     p->last_decoded = p->last_submitted = 0;
     p->has_prev = false;
     clear_ready(p);
+    return CUSAT_OK;
+}
+
+int cusat_rx_pool_set_copy_threads(cusat_rx_pool* p, int helpers)
+{
+    if (!p || helpers < 0 || helpers > 32)
+        return fail(CUSAT_ERR_ARG, "invalid copy thread count");
+    std::shared_ptr<CopyCrew> crew = helpers ? std::make_shared<CopyCrew>(helpers) : nullptr;
+    if (p->mix)
+        p->mix->crew = crew;
+    for (PoolEntry& e : p->chains)
+        e.chain->crew = crew;  // one crew: the pool submits to one chain at a time
     return CUSAT_OK;
 }
 

@@ -415,6 +415,11 @@ int cusat_rx_chain_set_weights(cusat_rx_chain* c, const int16_t* weights, int n_
 int cusat_rx_chain_set_decode_budget(cusat_rx_chain* c, const cusat_decode_budget* b);
 int cusat_rx_chain_set_launch_lock(cusat_rx_chain* c, void (*lock)(void*), void (*unlock)(void*), void* ctx);
 void cusat_rx_chain_set_block_when_full(cusat_rx_chain* c, int on);
+/* No counterpart in the reference (opt-in; 0, the default, copies on the
+ * submitting thread as the reference does): split each frame's copy into the
+ * pinned ring across `helpers` extra threads, which spin while frames keep
+ * coming and sleep after 0.5 ms without one. */
+int cusat_rx_chain_set_copy_threads(cusat_rx_chain* c, int helpers);
 void cusat_rx_chain_update_snr(cusat_rx_chain* c, float snr_db);
 /* symbols: n_symbols complex (re, im) host values; copied before return */
 int cusat_rx_chain_submit_xfecframe(cusat_rx_chain* c, const float* symbols, int n_symbols);
@@ -468,6 +473,8 @@ int cusat_rx_pool_launch_stale(cusat_rx_pool* p, double max_age_ms);
 int cusat_rx_pool_reset_all(cusat_rx_pool* p);
 int cusat_rx_pool_warmup_all(cusat_rx_pool* p);
 void cusat_rx_pool_update_snr(cusat_rx_pool* p, int modcod, float snr_db);
+/* As cusat_rx_chain_set_copy_threads, for every chain of the pool. */
+int cusat_rx_pool_set_copy_threads(cusat_rx_pool* p, int helpers);
 int cusat_rx_pool_set_launch_lock(cusat_rx_pool* p, void (*lock)(void*), void (*unlock)(void*), void* ctx);
 /* out[0..4] = total frames, total errors, total GPU drops, max_output_bytes,
  * data SNR (dB) of the last decoded MODCOD */

@@ -356,6 +356,8 @@ class rx_fec_chain
     void warmup() { ok(cusat_rx_chain_warmup(c_), "warmup"); }
     void update_snr(float snr_db) { cusat_rx_chain_update_snr(c_, snr_db); }
     void set_block_when_full(bool on) { cusat_rx_chain_set_block_when_full(c_, on ? 1 : 0); }
+    // extension (not in the reference): frame copies split across helper threads
+    void set_copy_threads(int helpers) { ok(cusat_rx_chain_set_copy_threads(c_, helpers), "set_copy_threads"); }
     void set_diag_fec_bench(bool) {}
     void set_diag_llr_histogram(bool) {}
     void set_diag_ldpc_convergence(bool) {}
@@ -498,6 +500,7 @@ class rx_fec_pool
             cusat_rx_pool_set_launch_lock(p_, nullptr, nullptr, nullptr);
     }
     void update_snr(uint8_t modcod, float snr_db) { cusat_rx_pool_update_snr(p_, modcod, snr_db); }
+    void set_copy_threads(int helpers) { ok(cusat_rx_pool_set_copy_threads(p_, helpers), "set_copy_threads"); }
     int max_output_bytes() const { return (int)stat(3); }
     uint64_t total_frame_count() const { return (uint64_t)stat(0); }
     uint64_t total_error_count() const { return (uint64_t)stat(1); }

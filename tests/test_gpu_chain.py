@@ -105,13 +105,16 @@ def run_chain(chain, frames):
     return np.concatenate(out), dfl
 
 
-@pytest.mark.parametrize("name,fs,n,mb,streams", [("qpsk1/2", SHORT, 45, 4, 2), ("8psk3/5", SHORT, 40, 8, 3),
-                                                  ("8psk3/5", NORMAL, 36, 5, 4)])
-def test_chain_matches_oracle(cuda, name, fs, n, mb, streams):
+@pytest.mark.parametrize("name,fs,n,mb,streams,helpers", [("qpsk1/2", SHORT, 45, 4, 2, 0),
+                                                          ("qpsk1/2", SHORT, 45, 4, 2, 2),
+                                                          ("8psk3/5", SHORT, 40, 8, 3, 0),
+                                                          ("8psk3/5", NORMAL, 36, 5, 4, 3)])
+def test_chain_matches_oracle(cuda, name, fs, n, mb, streams, helpers):
     _, mod, rate, _, _, thr = E.find_modcod(name)
     frames = traffic(mod, rate, fs, n, thr + 0.8, seed=n + mb)
     chain = cs.rx_fec_chain(fs, rate, mod, 50, 64, streams, mb)
     chain.set_decode_budget(cs.gpu_decode_budget(0))
+    chain.set_copy_threads(helpers)           # frame copies split across helper threads (or not)
     ref = OracleChain(mod, rate, fs, mb, 50)
     ref.start_from(chain, thr + 0.8)
     out, dfl = run_chain(chain, frames)
@@ -286,6 +289,7 @@ def test_mixed_pool_equals_per_modcod_pool(cuda, monkeypatch, pattern):
         used[m] += 1
     per = cs.rx_fec_pool(SHORT, mods, 50, 64, 2, 4)
     mix = cs.rx_fec_pool(SHORT, mods, 50, 64, 2, 4, mixed=True, slot_frames=16)
+    mix.set_copy_threads(2)
     for p in (per, mix):
         p.warmup_all()
         for idx in mods:
