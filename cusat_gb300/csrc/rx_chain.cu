@@ -1369,7 +1369,8 @@ int cusat_rx_pool_create_mixed(int framesize, const int32_t* modcods, int n_modc
     }
     p->mix.reset(x);
     p->budget.s = x->budget;
-    p->max_output_bytes = x->max_kbch * micro_batch * kFlight;
+    // a block holds at most one slot's frames
+    p->max_output_bytes = x->max_kbch * std::max(micro_batch * kFlight, slot_frames);
     *out = p;
     return CUSAT_OK;
 }
