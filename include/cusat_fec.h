@@ -76,7 +76,9 @@ int cusat_ldpc_decoder_set_weights(cusat_ldpc_decoder* dec, const int16_t* weigh
  * .cu:1324-1336): decodes `batch` frames of n_bits int16 LLRs read from
  * device memory, asynchronously on `stream`.  hard_out (batch*k_bytes) and
  * trials_out (batch) are device or mapped pinned pointers; NULL selects the
- * decoder's internal pinned buffers (read them with _results after a sync). */
+ * decoder's internal pinned buffers (read them with _results after a sync).
+ * One launch at a time per decoder object (its message scratch), as with
+ * the reference's instances. */
 int cusat_ldpc_decode_launch(cusat_ldpc_decoder* dec, const int16_t* soft_dev, int batch,
                              void* stream, uint8_t* hard_out, int32_t* trials_out);
 
@@ -180,7 +182,10 @@ int cusat_rx_fec_info(const cusat_rx_fec* rx, int32_t* out);
 int cusat_rx_fec_set_weights(cusat_rx_fec* rx, const int16_t* weights, int n_iter);
 float cusat_rx_fec_capped_llr_gain(const cusat_rx_fec* rx, float llr_gain);
 /* Symbols on the device in, results to device or mapped pinned memory;
- * llr_gain is capped like demap_batch does (demapper_kernel.cu:283-291). */
+ * llr_gain is capped like demap_batch does (demapper_kernel.cu:283-291).
+ * The object's LLR and message scratch serve one launch at a time: launches
+ * of one object on different streams must not overlap (one object per
+ * stream, as the reference's chain keeps one instance per stream). */
 int cusat_rx_fec_launch(cusat_rx_fec* rx, const float* sym_dev, int batch, float noise_var,
                         float llr_gain, uint8_t* hard_out, int32_t* trials_out,
                         int32_t* bch_valid_out, void* stream);
@@ -218,7 +223,9 @@ int cusat_batch_info(const cusat_batch* b, int32_t* out);
  * for later launches and for replays of an existing capture. */
 int cusat_batch_set_weights(cusat_batch* b, int modcod, const int16_t* weights, int n_iter);
 /* Decodes n frames on `stream` (waits for the previous launch's descriptor
- * copies first; the frames' buffers must stay valid until completion). */
+ * copies first; the frames' buffers must stay valid until completion).  One
+ * launch (or replay) at a time per batch object: they share its LLR and
+ * message scratch. */
 int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* stream);
 /* Times reps launches of each candidate (class order x grid split) on this
  * frame list and keeps the fastest for later launches and captures. */
