@@ -192,7 +192,6 @@ int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, c
         if (!cnt)
             continue;
         CU(cudaStreamWaitEvent(c.stream, b->fork, 0), "cudaStreamWaitEvent");
-        CU(cudaMemsetAsync(c.queue, 0, sizeof(unsigned int), c.stream), "cudaMemsetAsync(queue)");
         cusat::DecodeArgs a = c.proto;
         a.frames = d_frames + b->class_off[k];
         a.n_frames = cnt;
@@ -303,6 +302,8 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
             e = cudaMalloc(&c.msg, (size_t)c.grid_max * msg_cta);
         if (e == cudaSuccess)
             e = cudaMalloc(&c.queue, 256);
+        if (e == cudaSuccess)
+            e = cudaMemset(c.queue, 0, 256);  // the decoder rearms it after each launch
         if (e == cudaSuccess)
             e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess)

@@ -85,6 +85,7 @@ struct Engine {
         const size_t msg_bytes = (size_t)grid_max * p->R * p->msg_row;
         CU(cudaMalloc(&msg, msg_bytes), "cudaMalloc(messages)");
         CU(cudaMalloc(&queue, 256), "cudaMalloc(queue)");
+        CU(cudaMemset(queue, 0, 256), "cudaMemset(queue)");  // the kernel rearms it after each launch
         proto.msg = msg;
         proto.msg_stride = p->R * p->msg_row / 16;
         proto.queue = queue;
@@ -95,7 +96,6 @@ struct Engine {
     {
         a.n_frames = batch;
         const int grid = batch < grid_max ? batch : grid_max;
-        CU(cudaMemsetAsync(queue, 0, sizeof(unsigned int), stream), "cudaMemsetAsync(queue)");
         const int rc = cusat::launch_decoder(fn, a, grid, threads, stream);
         if (rc != 0)
             return cuda_fail((cudaError_t)rc, "decoder launch");

@@ -64,7 +64,7 @@ struct DecodeArgs {
     int32_t* trials;         // single code: [n_frames]
     uint4* msg;              // [gridDim.x][msg_stride] scratch
     int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
-    unsigned int* queue;     // frame counter, zero at launch
+    unsigned int* queue;     // [0] frame counter, [1] CTAs done: zero at launch, zeroed again by the last CTA
     // shared-memory carve-up (bytes)
     int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_code, sm_misc, sm_msgbuf,
         sm_total;
@@ -587,6 +587,17 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), min_ctas_per_sm(C
             decode_frame<CMAX, LANES, true>(a, c, smem, stage, t, job);
         else
             decode_frame<CMAX, LANES, false>(a, c, smem, stage, t, job);
+    }
+    // The last CTA out rearms the counters for the next launch (no memset
+    // before each launch or graph replay): every CTA has drawn its final
+    // ticket before its fenced exit count, so none reads the counter after
+    // the reset.
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(a.queue + 1, 1u) == gridDim.x - 1) {
+            atomicExch(a.queue, 0u);
+            atomicExch(a.queue + 1, 0u);
+        }
     }
 }
 

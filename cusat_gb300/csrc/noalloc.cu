@@ -200,8 +200,9 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
         grid = batch;
     if (grid < 1)
         return fail(CUSAT_ERR_UNSUPPORTED, "decoder kernel cannot be resident");
-    // the frame counter must start at zero on every call
-    e = cudaMemsetAsync(st.queue, 0, sizeof(unsigned int), s);
+    // frame and exit counters start at zero (the kernel also rearms them on
+    // exit; zeroed here as well since nothing else owns these arrays)
+    e = cudaMemsetAsync(st.queue, 0, 2 * sizeof(unsigned int), s);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaMemsetAsync(frame counter)");
     const int rc = cusat::launch_decoder(fn, a, grid, threads, s);

@@ -108,7 +108,8 @@ def run_chain(chain, frames):
 @pytest.mark.parametrize("name,fs,n,mb,streams,helpers", [("qpsk1/2", SHORT, 45, 4, 2, 0),
                                                           ("qpsk1/2", SHORT, 45, 4, 2, 2),
                                                           ("8psk3/5", SHORT, 40, 8, 3, 0),
-                                                          ("8psk3/5", NORMAL, 36, 5, 4, 3)])
+                                                          ("8psk3/5", NORMAL, 36, 5, 4, 3),
+                                                          ("16apsk2/3", SHORT, 40, 8, 2, 1)])
 def test_chain_matches_oracle(cuda, name, fs, n, mb, streams, helpers):
     _, mod, rate, _, _, thr = E.find_modcod(name)
     frames = traffic(mod, rate, fs, n, thr + 0.8, seed=n + mb)
