@@ -787,7 +787,8 @@ struct MixPool {
     int submit_idx = 0, launch_idx = 0, drain_idx = 0, next_lane = 0, fill = 0;
     int open_mc = -1;                          // MODCOD of the open virtual micro-batch
     std::vector<std::pair<int, int>> open_at;  // its frames: (slot submit index, frame)
-    Clock::time_point open_start{};
+    Clock::time_point open_start{};            // its first frame's submission
+    Clock::time_point slot_start{};            // the current slot's first frame's submission
     std::shared_ptr<BudgetState> budget;
     void (*lock_fn)(void*) = nullptr;
     void (*unlock_fn)(void*) = nullptr;
@@ -1070,6 +1071,41 @@ void mix_seal(MixPool& x)
     }
 }
 
+// Submits the current slot without the open micro-batch's frames at its end,
+// which move to the start of the next slot (symbols copied, references
+// updated); returns 1 if frames were submitted.
+int mix_split(MixPool& x)
+{
+    int first = x.fill;
+    for (const auto& at : x.open_at)
+        if (at.first == x.submit_idx)
+            first = std::min(first, at.second);
+    if (first == 0 || x.submit_idx + 1 - x.drain_idx >= kFlight - 2)
+        return 0;  // nothing closed to launch, or no free slot
+    MixSlot& cur = x.slot(x.submit_idx);
+    MixSlot& nxt = x.slot(x.submit_idx + 1);
+    const int n_move = x.fill - first;
+    for (int k = 0; k < n_move; k++) {
+        memcpy(nxt.sym + (size_t)k * x.max_xfec * 2, cur.sym + (size_t)(first + k) * x.max_xfec * 2,
+               (size_t)x.mc[cur.modcod[first + k]].xfec * 2 * sizeof(float));
+        nxt.modcod[k] = cur.modcod[first + k];
+    }
+    cur.n_frames = first;
+    cur.open -= n_move;
+    nxt.n_frames = n_move;
+    nxt.open = n_move;
+    nxt.in_flight = false;
+    for (auto& at : x.open_at)
+        if (at.first == x.submit_idx) {
+            at.first++;
+            at.second -= first;
+        }
+    x.submit_idx++;
+    x.fill = n_move;
+    x.slot_start = x.open_start;
+    return 1;
+}
+
 int mix_finish(cusat_rx_pool* p)
 {
     MixPool& x = *p->mix;
@@ -1111,14 +1147,19 @@ int mix_submit(cusat_rx_pool* p, const float* symbols, int n_symbols, int modcod
             return rc;
     }
     MixModcod& m = x.mc[mi];
+    // a MODCOD change closes the previous MODCOD's micro-batch even when this
+    // frame is then dropped (the reference flushes that chain first)
+    if (x.open_mc >= 0 && x.open_mc != mi)
+        mix_close(x);
     if (x.submit_idx - x.drain_idx >= kFlight - 2 || n_symbols != m.xfec) {
         m.drops++;
         m.frames++;
         m.errors++;
+        const int rc = mix_pump(x, false);  // the closed frames may complete a slot
+        if (rc)
+            return rc;
         return p->ready.empty() ? 0 : 1;
     }
-    if (x.open_mc >= 0 && x.open_mc != mi)
-        mix_close(x);
     MixSlot& t = x.slot(x.submit_idx);
     const int k = x.fill;
     float* dest = t.sym + (size_t)k * x.max_xfec * 2;
@@ -1129,6 +1170,8 @@ int mix_submit(cusat_rx_pool* p, const float* symbols, int n_symbols, int modcod
     }
     t.modcod[k] = mi;
     t.open++;
+    if (k == 0)
+        x.slot_start = Clock::now();
     if (x.open_at.empty())
         x.open_start = Clock::now();
     x.open_mc = mi;
@@ -1508,14 +1551,21 @@ int cusat_rx_pool_launch_stale(cusat_rx_pool* p, double max_age_ms)
         MixPool& x = *p->mix;
         if (x.failed)
             return x.failed;
-        if (!x.open_at.empty() &&
-            std::chrono::duration<double, std::milli>(now - x.open_start).count() >= max_age_ms) {
+        auto age_ms = [&](Clock::time_point t0) { return std::chrono::duration<double, std::milli>(now - t0).count(); };
+        if (!x.open_at.empty() && age_ms(x.open_start) >= max_age_ms) {
+            // the open micro-batch is stale (the reference launches it): close
+            // it and launch the partial slot
             mix_seal(x);
-            const int rc = mix_pump(x, false);
-            if (rc)
-                return rc;
             launched = 1;
+        } else if (x.fill > 0 && age_ms(x.slot_start) >= max_age_ms) {
+            // frames of earlier micro-batches wait in the partial slot (the
+            // reference launched them at their MODCOD change or when full):
+            // launch them, the open micro-batch moves on to a new slot
+            launched = mix_split(x);
         }
+        const int rc = mix_pump(x, false);
+        if (rc)
+            return rc;
         return launched;
     }
     for (PoolEntry& e : p->chains) {

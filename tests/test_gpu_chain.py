@@ -323,3 +323,30 @@ def test_mixed_pool_stale_launch_and_reset(cuda):
     assert pool.chain(4) is None
     pool.reset_all()
     assert pool.total_frame_count() == 0
+
+
+def test_mixed_pool_stale_slot_split(cuda):
+    """A partial slot whose frames are stale but whose open micro-batch is
+    fresh: launch_stale launches the closed frames now (the reference
+    launched them at their MODCOD change or when full) and carries the open
+    micro-batch into the next slot."""
+    import time
+    pool = cs.rx_fec_pool(SHORT, [4], 50, 64, 2, 4, mixed=True, slot_frames=64)
+    pool.warmup_all()
+    mm = E.modcod_by_index(4)
+    pool.update_snr(4, mm[5] + 1.0)
+    fr = traffic(mm[1], mm[2], SHORT, 6, mm[5] + 1.0, seed=8)   # frame 2 is sent 4 dB lower
+    for f in fr[:4]:
+        pool.submit(f, 4)                     # one full (closed) micro-batch in the partial slot
+    time.sleep(0.3)
+    pool.submit(fr[4], 4)                     # a new micro-batch opens
+    assert pool.launch_stale(150.0) is True   # slot 300 ms old, open micro-batch fresh
+    for _ in range(2000):
+        pool.drain_all_completed()
+        if pool.modcod_counters(4)[0] == 4:
+            break
+        time.sleep(0.001)
+    assert pool.modcod_counters(4) == (4, 1)  # the closed four decoded, frame 4 still held
+    pool.submit(fr[5], 4)
+    pool.finish_all_pending()
+    assert pool.modcod_counters(4) == (6, 1)
