@@ -620,11 +620,18 @@ class rx_fec_chain:
     def get_gse_output(self, max_bytes=None):
         if max_bytes is None:
             max_bytes = self._max_out
-        out = np.empty(max(max_bytes, 1), np.uint8)
+        out = self._out_buffer(max_bytes)
         n = _capi.lib().cusat_rx_chain_get_gse_output(self._h, out.ctypes.data, max_bytes)
         if n < 0:
             _capi.check(n)
         return out[:n].copy()
+
+    def _out_buffer(self, n):
+        # one buffer per object, reused: outputs are copied out of it
+        buf = getattr(self, "_buf", None)
+        if buf is None or buf.size < max(n, 1):
+            buf = self._buf = np.empty(max(n, 1), np.uint8)
+        return buf
 
     def gse_dfl_sizes(self):
         n = _capi.lib().cusat_rx_chain_gse_dfl_sizes(self._h, None, 0)
@@ -737,6 +744,7 @@ class rx_fec_pool:
                                                          ctypes.byref(h)))
         self._h = h
         self.mixed = bool(mixed)
+        self._max_out = self.max_output_bytes()
         self.modcods = [int(i) for i in enabled_modcods]
 
     def close(self):
@@ -758,12 +766,14 @@ class rx_fec_pool:
 
     def get_gse_output(self, max_bytes=None):
         if max_bytes is None:
-            max_bytes = self.max_output_bytes()
-        out = np.empty(max(max_bytes, 1), np.uint8)
-        n = _capi.lib().cusat_rx_pool_get_gse_output(self._h, out.ctypes.data, max_bytes)
+            max_bytes = self._max_out
+        buf = getattr(self, "_buf", None)
+        if buf is None or buf.size < max(max_bytes, 1):
+            buf = self._buf = np.empty(max(max_bytes, 1), np.uint8)  # reused across calls
+        n = _capi.lib().cusat_rx_pool_get_gse_output(self._h, buf.ctypes.data, max_bytes)
         if n < 0:
             _capi.check(n)
-        return out[:n].copy()
+        return buf[:n].copy()
 
     def gse_dfl_sizes(self):
         n = _capi.lib().cusat_rx_pool_gse_dfl_sizes(self._h, None, 0)
