@@ -868,6 +868,32 @@ CHAIN_SETTINGS = [(4, 8, -1, 0), (16, 8, -1, 0), (64, 4, -1, 0), (64, 4, 0, 0), 
                   (128, 4, -1, 3)]
 
 
+def chain_cpp_rows(cs, n, esn0):
+    """Builds tests/chain_timing.cc against the library and runs it for a few
+    chain settings; {} if no C++ compiler is available."""
+    exe = os.path.join(ROOT, "cusat_gb300", "_build", "chain_timing")
+    lib = cs.library_path()
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cmd = ["g++", "-std=c++17", "-O2", "-pthread", "-I", os.path.join(ROOT, "include"), "-I",
+           os.path.join(cuda, "include"), os.path.join(ROOT, "tests", "chain_timing.cc"), "-o", exe, lib,
+           "-L", os.path.join(cuda, "lib64"), "-L", os.path.join(cuda, "targets", "sbsa-linux", "lib"), "-lcudart",
+           "-Wl,-rpath," + os.path.dirname(lib)]
+    try:
+        subprocess.run(cmd, check=True, capture_output=True, timeout=300)
+    except (OSError, subprocess.SubprocessError):
+        return {}
+    rows = {}
+    for mb, streams, cap, helpers in [(4, 8, -1, 0), (128, 4, 0, 0), (128, 4, 0, 3), (128, 4, -1, 3)]:
+        r = subprocess.run([exe, str(n), str(mb), str(streams), str(cap), str(helpers), str(esn0)],
+                           capture_output=True, text=True, timeout=300)
+        try:
+            rows[f"micro_batch {mb}, {streams} streams, budget {'default' if cap < 0 else 'unlimited'}, "
+                 f"copy helpers {helpers}"] = json.loads(r.stdout.strip().splitlines()[-1])
+        except (ValueError, IndexError):
+            rows[f"micro_batch {mb}, {streams} streams"] = {"error": r.stderr[-200:]}
+    return rows
+
+
 def chain_main(args, torch, cs, rank, local_rank, world):
     """The frame-at-a-time receive chain (rx_fec_chain API) on the headline
     MODCOD: host XFECFRAMEs submitted one by one, micro-batched, launched on
@@ -911,6 +937,9 @@ def chain_main(args, torch, cs, rank, local_rank, world):
             "force_drains": chain.force_drain_count(), "errors": chain.frame_error_count()}
         chain.close()
         budget.close()
+    # the same chain driven from C++ through the rx_fec_chain shim
+    # (include/cusat_fec.hpp; tests/chain_timing.cc), no Python in the loop
+    cpp_rows = chain_cpp_rows(cs, args.steps * wl["frames"], wl["esn0_db"])
     clk = clocks.stop()
     # where a submit's host time goes: copying one frame into a pinned buffer
     # (numpy), and the ctypes round trip of a trivial call
@@ -937,7 +966,7 @@ def chain_main(args, torch, cs, rank, local_rank, world):
         "config": {"workload": "rx_fec_chain: frames submitted one at a time from host memory, 256 per step, "
                                "max 50 iterations", "settings": rows,
                    "e2e_note": "host symbols in, per-frame verdicts and GSE data fields out (pinned)",
-                   "host_frame_copy_us": copy_us, "host_ctypes_call_us": call_us},
+                   "host_frame_copy_us": copy_us, "host_ctypes_call_us": call_us, "cpp": cpp_rows},
         "clocks": clk}), flush=True)
 
 
