@@ -232,6 +232,10 @@ def main():
         else:
             reference_arm(args, wl)
         return
+    if args.workload in ("chain", "acm"):
+        # many streams of small launches: more hardware work queues than the
+        # default 8 (process setting, must precede CUDA initialisation)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
     rank, local_rank, world = dist_env()
     torch.cuda.set_device(local_rank)
@@ -883,12 +887,13 @@ def chain_cpp_rows(cs, n, esn0):
     except (OSError, subprocess.SubprocessError):
         return {}
     rows = {}
-    for mb, streams, cap, helpers in [(4, 8, -1, 0), (128, 4, 0, 0), (128, 4, 0, 3), (128, 4, -1, 3)]:
-        r = subprocess.run([exe, str(n), str(mb), str(streams), str(cap), str(helpers), str(esn0)],
+    for mb, streams, cap, helpers, conn in [(4, 8, -1, 0, 8), (4, 8, -1, 0, 32), (4, 8, -1, 3, 32),
+                                            (128, 4, 0, 0, 32), (128, 4, 0, 3, 32), (128, 4, -1, 3, 32)]:
+        r = subprocess.run([exe, str(n), str(mb), str(streams), str(cap), str(helpers), str(esn0), str(conn)],
                            capture_output=True, text=True, timeout=300)
         try:
             rows[f"micro_batch {mb}, {streams} streams, budget {'default' if cap < 0 else 'unlimited'}, "
-                 f"copy helpers {helpers}"] = json.loads(r.stdout.strip().splitlines()[-1])
+                 f"copy helpers {helpers}, {conn} hardware queues"] = json.loads(r.stdout.strip().splitlines()[-1])
         except (ValueError, IndexError):
             rows[f"micro_batch {mb}, {streams} streams"] = {"error": r.stderr[-200:]}
     return rows
@@ -966,7 +971,8 @@ def chain_main(args, torch, cs, rank, local_rank, world):
         "config": {"workload": "rx_fec_chain: frames submitted one at a time from host memory, 256 per step, "
                                "max 50 iterations", "settings": rows,
                    "e2e_note": "host symbols in, per-frame verdicts and GSE data fields out (pinned)",
-                   "host_frame_copy_us": copy_us, "host_ctypes_call_us": call_us, "cpp": cpp_rows},
+                   "host_frame_copy_us": copy_us, "host_ctypes_call_us": call_us, "cpp": cpp_rows,
+                   "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")},
         "clocks": clk}), flush=True)
 
 

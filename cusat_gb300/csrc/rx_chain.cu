@@ -407,8 +407,17 @@ int cusat_rx_chain_create(int framesize, int rate, int modulation, int max_trial
     c->rate = rate;
     c->framesize = framesize;
     c->micro_batch = micro_batch;
-    c->n_streams = n_gpu_streams;
-    c->lanes.resize(n_gpu_streams);
+    // Launches on one stream run one after another, so n_gpu_streams
+    // micro-batches of micro_batch frames bound the frames in flight (32 at
+    // the reference's defaults, against 152 SMs).  The in-flight budget is
+    // what bounds residency: enough streams to fill the default budget (one
+    // frame per SM), never fewer than asked for.
+    {
+        const int cap = default_budget()->cap;
+        const int fill = cap > 0 ? (cap + micro_batch - 1) / micro_batch : n_gpu_streams;
+        c->n_streams = std::min(64, std::max(n_gpu_streams, fill));
+    }
+    c->lanes.resize(c->n_streams);
     c->flight.resize(kFlight);
     int32_t info[6];
     for (Lane& L : c->lanes) {

@@ -400,8 +400,10 @@ int cusat_dd_snr(int modulation, int rate, int framesize, const float* sym, int 
 /* One MODCOD's frame-at-a-time receive chain, replacing cusat_dsp::rx_fec_chain
  * (lib/cusat_dsp/rx_fec_chain.h:61-297) call for call: frames accumulate
  * into micro-batches in a 128-slot flight ring, each full micro-batch is
- * launched at once (within the decode budget) on the next of n_gpu_streams
- * streams, completed slots are drained in submission order into GSE output
+ * launched at once (within the decode budget) on the next of the chain's
+ * streams (n_gpu_streams, or more when that many micro-batches cannot fill
+ * the default in-flight budget: launches on one stream run one after
+ * another), completed slots are drained in submission order into GSE output
  * (the data fields of frames that converged, passed BCH and carry a valid
  * GSE BBHEADER) and per-frame data-field sizes.  Every 32nd submitted frame
  * re-estimates the SNR (decision-directed; pilot SNR for >= 128 points).
@@ -416,7 +418,8 @@ int cusat_rx_chain_create(int framesize, int rate, int modulation, int max_trial
                           int n_gpu_streams, int micro_batch, cusat_rx_chain** out);
 void cusat_rx_chain_destroy(cusat_rx_chain* c);
 /* out[0..5] = xfecframe_len, kbch_bytes, batch_size(), max_output_bytes(),
- * micro_batch, streams */
+ * micro_batch, streams in use (at least n_gpu_streams; enough to fill the
+ * default in-flight budget) */
 int cusat_rx_chain_info(const cusat_rx_chain* c, int32_t* out);
 int cusat_rx_chain_set_weights(cusat_rx_chain* c, const int16_t* weights, int n_iter);
 int cusat_rx_chain_set_decode_budget(cusat_rx_chain* c, const cusat_decode_budget* b);

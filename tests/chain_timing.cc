@@ -2,7 +2,7 @@
 // reference's receiver drives it: XFECFRAMEs submitted one by one from host
 // memory, output collected when reported, a final flush.  Used by
 // `bench.py --workload chain` for the C++ rows.
-//   chain_timing <frames> <micro_batch> <streams> <budget: -1 default, 0 none> <copy helpers> <esn0_db>
+//   chain_timing <frames> <micro_batch> <streams> <budget: -1 default, 0 none> <copy helpers> <esn0_db> [connections]
 // Prints one JSON object: frames, seconds, info Gbit/s, frame errors.
 #include <stdio.h>
 #include <stdlib.h>
@@ -20,6 +20,11 @@ int main(int argc, char** argv)
 {
     if (argc < 7)
         return 2;
+    // launches of many streams share CUDA_DEVICE_MAX_CONNECTIONS hardware
+    // queues (8 unless set before the first CUDA call): a receiver that runs
+    // small micro-batches on many streams raises it first
+    if (argc > 7)
+        setenv("CUDA_DEVICE_MAX_CONNECTIONS", argv[7], 1);
     const int n = atoi(argv[1]), mb = atoi(argv[2]), streams = atoi(argv[3]), cap = atoi(argv[4]),
               helpers = atoi(argv[5]);
     const float esn0 = (float)atof(argv[6]);
