@@ -100,9 +100,6 @@ int extract(cusat_bb_extractor* x, const uint8_t* hard_dev, int hard_stride, con
             const int32_t* trials_dev, const int32_t* bch_valid_dev, int batch, uint8_t* out_dev, int max_out,
             int32_t* lengths_dev, int32_t* offsets_dev, cudaStream_t s)
 {
-    static const bool carveout = (cusat::share_decoder_carveout(bb_header_kernel), cusat::share_decoder_carveout(bb_place_kernel),
-                                  cusat::share_decoder_carveout(bb_copy_kernel), true);
-    (void)carveout;
     bb_header_kernel<<<(batch + 255) / 256, 256, 0, s>>>(hard_dev, hard_stride, x->kbch, kbch_dev, trials_dev,
                                                          bch_valid_dev, x->prbs, batch, lengths_dev);
     CU(cudaGetLastError(), "BBHEADER launch");

@@ -34,8 +34,6 @@ template <int KIND, int NM>
 void launch_demap_kind(const DevDemap& d, const float2* sym, int batch, float noise_var, float llr_gain,
                        int16_t* out, cudaStream_t stream)
 {
-    static const bool carveout = (share_decoder_carveout(demap_kernel<KIND, NM>), true);
-    (void)carveout;
     const int per_block = kDemapThreads * span_of(KIND);
     for (int f0 = 0; f0 < batch; f0 += 65535) {
         dim3 grid((d.interleaved_len + per_block - 1) / per_block, batch - f0 < 65535 ? batch - f0 : 65535);
@@ -110,8 +108,7 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
 
 int launch_demap_mixed(const DevDemap* demaps, const DemapFrame* frames, int n, int max_len, cudaStream_t stream)
 {
-    static const bool carveout = (share_decoder_carveout(demap_mixed_kernel), true);
-    (void)carveout;
+
     const int per_block = kDemapThreads * kDemapSpan;
     for (int f0 = 0; f0 < n; f0 += 65535) {
         dim3 grid((max_len + per_block - 1) / per_block, n - f0 < 65535 ? n - f0 : 65535);
@@ -278,8 +275,6 @@ int launch_bch_check_mixed(const BchDev* codes, const BchFrame* frames, int n, c
 {
     if (n <= 0)
         return 0;
-    static const bool carveout = (share_decoder_carveout(bch_check_mixed_kernel), true);
-    (void)carveout;
     bch_check_mixed_kernel<<<(n + 3) / 4, 128, 0, stream>>>(codes, frames, n);
     return (int)cudaGetLastError();
 }
@@ -287,10 +282,6 @@ int launch_bch_check_mixed(const BchDev* codes, const BchFrame* frames, int n, c
 int launch_bch_check(const BchDev& t, const uint8_t* cw, int32_t* valid, uint8_t* rem, int batch,
                      cudaStream_t stream)
 {
-    static const bool carveout = (share_decoder_carveout(bch_check_kernel<1>), share_decoder_carveout(bch_check_kernel<2>),
-                                  share_decoder_carveout(bch_check_kernel<3>), share_decoder_carveout(bch_check_kernel<4>),
-                                  true);
-    (void)carveout;
     const int blocks = (batch + 3) / 4;
     if (t.words == 1)
         bch_check_kernel<1><<<blocks, 128, 0, stream>>>(t, cw, valid, rem, batch);

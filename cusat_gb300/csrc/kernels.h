@@ -47,17 +47,6 @@ SmemDims smem_dims_of(const DevCode& c, int lanes);
 int decoder_threads(int lanes);
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
 
-// Gives a small kernel the decoder's shared-memory carve-out (maximum shared,
-// once per kernel): kernels of the receive path interleave on many streams,
-// and an SM switching its L1/shared split between a decoder CTA and another
-// kernel's blocks must drain first.
-template <class F>
-inline void share_decoder_carveout(F* fn)
-{
-    cudaFuncSetAttribute(reinterpret_cast<const void*>(fn), cudaFuncAttributePreferredSharedMemoryCarveout,
-                         (int)cudaSharedmemCarveoutMaxShared);
-}
-
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream);
 // One frame of a mixed demap launch (device memory).
