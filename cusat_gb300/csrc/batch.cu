@@ -244,8 +244,6 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
         rc = upload_plan(*m->plan, &m->dp);
         if (rc == CUSAT_OK)
             rc = m->dm.init(m->mod, m->rate, m->fs);
-        if (rc == CUSAT_OK && m->dm.m.interleaved_len != m->dm.m.xfec)
-            rc = fail(CUSAT_ERR_UNSUPPORTED, "padded XFECFRAME");
         if (rc == CUSAT_OK)
             rc = m->bch.init(m->plan->gen, m->plan->p, (unsigned)(m->plan->n_bch / 8));
         if (rc)

@@ -541,8 +541,6 @@ int cusat_rx_fec_launch(cusat_rx_fec* r, const float* sym_dev, int batch, float 
         return fail(CUSAT_ERR_ARG, "null argument");
     if (batch <= 0 || batch > r->eng.max_batch)
         return fail(CUSAT_ERR_ARG, "batch outside 1..max_batch");
-    if (r->dm.m.interleaved_len != r->dm.m.xfec)
-        return fail(CUSAT_ERR_UNSUPPORTED, "padded XFECFRAME");
     // demap + deinterleave over the whole grid into HBM, then decode: the
     // decoder holds one frame per SM, and a demap inside it would run at one
     // CTA's memory parallelism

@@ -61,6 +61,10 @@ int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var
         launch_demap_kind<2, 5>(d, s, batch, noise_var, llr_gain, out, stream);
     else if (d.n_mod == 6)
         launch_demap_kind<2, 6>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_mod == 7)
+        launch_demap_kind<2, 7>(d, s, batch, noise_var, llr_gain, out, stream);
+    else if (d.n_mod == 8)
+        launch_demap_kind<2, 8>(d, s, batch, noise_var, llr_gain, out, stream);
     else
         launch_demap_kind<2, 0>(d, s, batch, noise_var, llr_gain, out, stream);
     return (int)cudaGetLastError();
@@ -83,7 +87,7 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
             pts[k] = d.points[k];
     __syncthreads();
     const bool full = d.n_points == 1 << d.n_mod;  // 2^n_mod points: the specialised log-MAP applies
-    const int sel = d.kind == 2 ? 2 * 16 + (full && d.n_mod >= 4 && d.n_mod <= 6 ? d.n_mod : 0) : d.kind * 16;
+    const int sel = d.kind == 2 ? 2 * 16 + (full && d.n_mod >= 4 && d.n_mod <= 8 ? d.n_mod : 0) : d.kind * 16;
     const int per_block = kDemapThreads * kDemapSpan;
     for (int j0 = blockIdx.x * per_block + threadIdx.x; j0 - (int)threadIdx.x < d.interleaved_len;
          j0 += gridDim.x * per_block) {
@@ -98,6 +102,8 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
                 case 36: demap_span<2, 4, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 case 37: demap_span<2, 5, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 case 38: demap_span<2, 6, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+                case 39: demap_span<2, 7, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
+                case 40: demap_span<2, 8, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 default: demap_span<2, 0, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 }
             }

@@ -162,12 +162,15 @@ __global__ void __launch_bounds__(kEncThreads) ldpc_encode_kernel(LdpcEnc e, uin
 
 struct MapArgs {
     int n_mod, xfec, stride;  // QPSK: bits 2j, 2j+1; otherwise column offsets, stride 1
+    int interleaved_len;      // symbols that carry frame bits (128APSK: xfec - 12)
+    int fec_bits;             // positions at or past it are stuffing bits (0)
     uint32_t col[8];
     const float2* points;     // by label
 };
 
 // Mapper: one thread per symbol; label bit b (MSB first) is frame bit
-// col[b] + j * stride.
+// col[b] + j * stride, 0 past the FECFRAME; padding symbols (128APSK) carry
+// the all-ones label (reference mapper.cc:42-62).
 __global__ void map_kernel(const uint8_t* __restrict__ cw, int cw_bytes, MapArgs m, float2* __restrict__ sym,
                            int batch)
 {
@@ -175,10 +178,14 @@ __global__ void map_kernel(const uint8_t* __restrict__ cw, int cw_bytes, MapArgs
     for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (size_t)gridDim.x * blockDim.x) {
         const int f = (int)(g / m.xfec), j = (int)(g - (size_t)f * m.xfec);
         const uint8_t* in = cw + (size_t)f * cw_bytes;
-        int label = 0;
-        for (int b = 0; b < m.n_mod; b++) {
-            const int pos = (int)m.col[b] + j * m.stride;
-            label |= ((in[pos >> 3] >> (7 - (pos & 7))) & 1) << (m.n_mod - 1 - b);
+        int label = (1 << m.n_mod) - 1;
+        if (j < m.interleaved_len) {
+            label = 0;
+            for (int b = 0; b < m.n_mod; b++) {
+                const int pos = (int)m.col[b] + j * m.stride;
+                if (pos < m.fec_bits)
+                    label |= ((in[pos >> 3] >> (7 - (pos & 7))) & 1) << (m.n_mod - 1 - b);
+            }
         }
         sym[g] = __ldg(m.points + label);
     }
@@ -219,7 +226,7 @@ int cusat_generator_create(int modulation, int rate, int framesize, int max_batc
     rc = g->bch.init(p->gen, p->p, (unsigned)(p->k_bch / 8));
     if (rc == CUSAT_OK)
         rc = g->dm.init(modulation, rate, framesize);
-    if (rc == CUSAT_OK && (g->dm.m.fec_len != p->N || g->dm.m.interleaved_len != g->dm.m.xfec))
+    if (rc == CUSAT_OK && g->dm.m.fec_len != p->N)
         rc = fail(CUSAT_ERR_UNSUPPORTED, "MODCOD and code do not match");
     if (rc == CUSAT_OK) {
         int n_addr = 0;
@@ -299,6 +306,8 @@ int cusat_generate(cusat_generator* g, const uint8_t* msg_dev, int batch, uint8_
         MapArgs m{};
         m.n_mod = d.n_mod;
         m.xfec = d.xfec;
+        m.interleaved_len = d.interleaved_len;
+        m.fec_bits = d.fec_len;
         m.stride = d.kind == 0 ? 2 : 1;
         for (int b = 0; b < 8; b++)
             m.col[b] = d.kind == 0 ? (uint32_t)b : d.col[b];

@@ -6,7 +6,6 @@
 // (lib/cusat_dsp/modulation/constellation.cc); every point is produced with
 // the same float/double arithmetic so that the points are bit-identical to
 // the reference's (checked against the reference host code in the tests).
-// 128APSK and the coordinate-table 256APSK rates are not built here.
 #include <math.h>
 
 #include <cmath>
@@ -23,6 +22,8 @@ extern "C" {
 namespace cusat {
 
 namespace {
+
+#include "gen/apsk256_points.inc"
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -270,6 +271,85 @@ void build_8apsk(std::vector<float>* p, int rate)
         polar(p, l, radius[l], angle[l] * kPi);
 }
 
+// 128APSK (EN 302 307-2 Tables 14a/14b): six rings; a label is q p r4..r0,
+// row r of 32 sits on one ring at first-quadrant angle a/d (units of pi),
+// mirrored into the quadrants (p, q) = 00, 01, 10, 11 as a, 2 - a, 1 - a,
+// 1 + a.  Each row is stored as {ring, a, d} with integer a, d; the four
+// angles are (a, 2d - a, d - a, d + a) / d, the table's own fractions.
+// (reference modulation/constellation.cc:347-398)
+void build_128apsk(std::vector<float>* p, int rate)
+{
+    static const int ROWS[32][3] = {
+        {0, 83, 1260},  {5, 11, 105},    {5, 37, 1680},  {5, 11, 168},   {1, 121, 2520},  {2, 23, 280},
+        {4, 19, 720},   {3, 61, 720},    {0, 103, 560},  {5, 61, 420},   {5, 383, 1680},  {5, 929, 5040},
+        {1, 113, 560},  {2, 169, 1008},  {4, 563, 2520}, {3, 139, 840},  {0, 243, 560},   {5, 1993, 5040},
+        {5, 43, 90},    {5, 73, 168},    {1, 1139, 2520}, {2, 117, 280}, {4, 341, 720},   {3, 349, 840},
+        {0, 177, 560},  {5, 1789, 5040}, {5, 49, 180},   {5, 53, 168},   {1, 167, 560},   {2, 239, 720},
+        {4, 199, 720},  {3, 281, 840},
+    };
+    const double ratio[6] = {1.0, 1.715, 2.118, 2.681, 2.75, rate == CUSAT_RATE_135_180 ? 3.819 : 3.733};
+    static const int COUNTS[6] = {16, 16, 16, 16, 16, 48};
+    double e = 0.0;
+    for (int i = 0; i < 6; i++)
+        e += COUNTS[i] * ratio[i] * ratio[i];
+    const double scale = sqrt(128.0 / e);
+    for (int row = 0; row < 32; row++) {
+        const float radius = (float)(ratio[ROWS[row][0]] * scale);
+        const int a = ROWS[row][1], d = ROWS[row][2];
+        const int num[4] = {a, 2 * d - a, d - a, d + a};
+        for (int col = 0; col < 4; col++) {
+            const int pp = col >> 1, qq = col & 1;
+            polar(p, (qq << 6) | (pp << 5) | row, radius, (double)num[col] / d * kPi);
+        }
+    }
+}
+
+// 256APSK: the rates 20/30 and 22/30 (and 132/180, which shares 22/30's
+// points) by the coordinates of EN 302 307-2 Table 15d, renormalised to unit
+// energy; the others on eight rings of 32 points (Tables 15a-15c), label
+// = x2 x1 x0 q p a2 a1 a0 with ring RING_OF[x] and angle (2 K_OF[a] - 1)
+// pi / 32 mirrored by (p, q).  (reference modulation/constellation.cc:400-444)
+void build_256apsk(std::vector<float>* p, int rate)
+{
+    const float* c = rate == CUSAT_RATE_20_30 ? cusat_apsk256_20_30
+                     : (rate == CUSAT_RATE_132_180 || rate == CUSAT_RATE_22_30) ? cusat_apsk256_22_30
+                                                                              : nullptr;
+    if (c) {
+        double e = 0.0;
+        for (int i = 0; i < 256; i++)
+            e += (double)c[2 * i] * c[2 * i] + (double)c[2 * i + 1] * c[2 * i + 1];
+        const float s = (float)sqrt(256.0 / e);
+        for (int i = 0; i < 256; i++)
+            put(p, i, c[2 * i] * s, c[2 * i + 1] * s);
+        return;
+    }
+    double g[7] = {1.791, 2.405, 2.980, 3.569, 4.235, 5.078, 6.536};
+    if (rate == CUSAT_RATE_128_180 || rate == CUSAT_RATE_135_180) {
+        const double common[5] = {1.794, 2.409, 2.986, 3.579, 4.045};
+        for (int i = 0; i < 5; i++)
+            g[i] = common[i];
+        g[5] = rate == CUSAT_RATE_128_180 ? 4.6 : 4.5;
+        g[6] = rate == CUSAT_RATE_128_180 ? 5.4 : 5.2;
+    }
+    const double ratio[8] = {1.0, g[0], g[1], g[2], g[3], g[4], g[5], g[6]};
+    double e = 0.0;
+    for (int i = 0; i < 8; i++)
+        e += 32.0 * ratio[i] * ratio[i];
+    const double scale = sqrt(256.0 / e);
+    static const int RING_OF[8] = {0, 1, 3, 2, 7, 6, 4, 5};
+    static const int K_OF[8] = {1, 2, 4, 3, 8, 7, 5, 6};
+    for (int x = 0; x < 8; x++) {
+        const float radius = (float)(ratio[RING_OF[x]] * scale);
+        for (int qq = 0; qq < 2; qq++)
+            for (int pp = 0; pp < 2; pp++)
+                for (int a = 0; a < 8; a++) {
+                    const double phi = (2 * K_OF[a] - 1) * kPi / 32.0;
+                    const double angle = pp ? (qq ? kPi + phi : kPi - phi) : (qq ? -phi : phi);
+                    polar(p, (x << 5) | (qq << 4) | (pp << 3) | a, radius, angle);
+                }
+    }
+}
+
 bool is_16apsk_8_8(int r)
 {
     return r == CUSAT_RATE_90_180 || r == CUSAT_RATE_96_180 || r == CUSAT_RATE_100_180 ||
@@ -339,6 +419,8 @@ int make_constellation(int mod, int rate, int framesize, std::vector<float>* p)
     case CUSAT_MOD_16APSK: bits = 4; break;
     case CUSAT_MOD_32APSK: bits = 5; break;
     case CUSAT_MOD_64APSK: bits = 6; break;
+    case CUSAT_MOD_128APSK: bits = 7; break;
+    case CUSAT_MOD_256APSK: bits = 8; break;
     default: return -1;
     }
     p->assign(2 << bits, 0.0f);
@@ -373,6 +455,8 @@ int make_constellation(int mod, int rate, int framesize, std::vector<float>* p)
             build_32apsk_4_12_16(p, rate);
         break;
     case CUSAT_MOD_64APSK: build_64apsk(p, rate); break;
+    case CUSAT_MOD_128APSK: build_128apsk(p, rate); break;
+    case CUSAT_MOD_256APSK: build_256apsk(p, rate); break;
     }
     return bits;
 }
@@ -407,14 +491,21 @@ bool build_modcod_demap(int mod, int rate, int framesize, ModcodDemap* d, std::s
     d->framesize = framesize;
     const int bits = make_constellation(mod, rate, framesize, &d->pts);
     if (bits < 0) {
-        if (err) *err = "modulation not supported (128APSK/256APSK are not built)";
+        if (err) *err = "modulation not supported";
         return false;
     }
     d->n_mod = bits;
     d->n_points = 1 << bits;
     d->fec_len = cusat_fecframe_bits(framesize);
-    d->xfec = d->fec_len / bits;
-    d->interleaved_len = d->xfec;
+    // 128APSK: 6 stuffing bits ahead of the interleaver and 12 padding
+    // symbols after it (reference cuda/demapper_kernel.cu:241-247)
+    if (mod == CUSAT_MOD_128APSK) {
+        d->interleaved_len = (d->fec_len + 6) / bits;
+        d->xfec = d->interleaved_len + 12;
+    } else {
+        d->xfec = d->fec_len / bits;
+        d->interleaved_len = d->xfec;
+    }
     d->kind = mod == CUSAT_MOD_QPSK ? 0 : mod == CUSAT_MOD_8PSK ? 1 : 2;
     uint32_t rows;
     if (make_interleaver(mod, rate, framesize, d->col, &rows) < 0) {
@@ -469,10 +560,17 @@ void map_frames(const ModcodDemap& d, const uint8_t* cw, int B, float* sym)
         const uint8_t* in = cw + (size_t)f * cw_bytes;
         float* out = sym + (size_t)f * d.xfec * 2;
         for (int j = 0; j < d.xfec; j++) {
-            int label = 0;
-            for (int b = 0; b < d.n_mod; b++) {
-                const int pos = (int)col[b] + j * stride;
-                label |= ((in[pos >> 3] >> (7 - (pos & 7))) & 1) << (d.n_mod - 1 - b);
+            // stuffing bits (positions past the FECFRAME) are 0; padding
+            // symbols (128APSK) carry the all-ones label (reference
+            // mapper.cc:42-62)
+            int label = d.n_points - 1;
+            if (j < d.interleaved_len) {
+                label = 0;
+                for (int b = 0; b < d.n_mod; b++) {
+                    const int pos = (int)col[b] + j * stride;
+                    if (pos < d.fec_len)
+                        label |= ((in[pos >> 3] >> (7 - (pos & 7))) & 1) << (d.n_mod - 1 - b);
+                }
             }
             out[2 * j] = d.pts[2 * label];
             out[2 * j + 1] = d.pts[2 * label + 1];

@@ -3,7 +3,7 @@
 Numeric values equal the reference's enums
 (lib/cusat_dsp/include/cusat_dsp/modcod_types.h:14-95) so that values pass
 through the C ABI unchanged.  MODCODS restates the reference's MODCOD table
-(lib/cusat_dsp/acm_config.h:53-116): index, modulation, rate, name and the
+(lib/cusat_dsp/acm_config.h:53-121): index, modulation, rate, name and the
 Es/N0 at which the reference measured post-BCH FER <= 1e-5 with normal
 frames, 25 iterations and AWGN.
 """
@@ -67,6 +67,10 @@ MODCODS = [
     (29, MOD_64APSK, 35, "64apsk11/15", 4.40, 15.00), (30, MOD_64APSK, 37, "64apsk7/9", 4.67, 15.60),
     (31, MOD_64APSK, 7, "64apsk4/5", 4.80, 16.10), (35, MOD_64APSK, 8, "64apsk5/6", 4.98, 17.23),
     (36, MOD_64APSK, 32, "64apsk32/45", 4.27, 14.18),
+    (32, MOD_128APSK, 36, "128apsk3/4", 5.25, 18.00), (34, MOD_128APSK, 38, "128apsk7/9", 5.44, 18.89),
+    (37, MOD_256APSK, 36, "256apsk3/4", 6.00, 23.34), (38, MOD_256APSK, 32, "256apsk32/45", 5.69, 22.40),
+    (39, MOD_256APSK, 27, "256apsk29/45", 5.16, 20.20), (40, MOD_256APSK, 29, "256apsk31/45", 5.51, 21.50),
+    (41, MOD_256APSK, 28, "256apsk2/3", 5.06, 18.10), (42, MOD_256APSK, 34, "256apsk11/15", 5.50, 19.80),
 ]
 
 

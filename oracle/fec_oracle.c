@@ -735,17 +735,20 @@ int orc_demap(const float* sym, int B, int xfec, int interleaved_len, int fec_le
 /* Mapper (reference cuda/mapper_kernel.cu:22-51, mapper.cc:75-86)           */
 /* ------------------------------------------------------------------------ */
 
-int orc_map(const uint8_t* cw, int B, int cw_bytes, int xfec, int n_mod, const uint32_t* col,
-            int stride, const float* pts_re, const float* pts_im, float* sym)
+int orc_map(const uint8_t* cw, int B, int cw_bytes, int xfec, int interleaved_len, int fec_len, int n_mod,
+            const uint32_t* col, int stride, const float* pts_re, const float* pts_im, float* sym)
 {
     for (int f = 0; f < B; f++) {
         const uint8_t* in = cw + (size_t)f * cw_bytes;
         for (int j = 0; j < xfec; j++) {
-            int label = 0;
-            for (int b = 0; b < n_mod; b++) {
-                const int pos = (int)col[b] + j * stride;
-                const int bit = (in[pos >> 3] >> (7 - (pos & 7))) & 1;
-                label |= bit << (n_mod - 1 - b);
+            int label = (1 << n_mod) - 1;
+            if (j < interleaved_len) {
+                label = 0;
+                for (int b = 0; b < n_mod; b++) {
+                    const int pos = (int)col[b] + j * stride;
+                    const int bit = pos < fec_len ? (in[pos >> 3] >> (7 - (pos & 7))) & 1 : 0;
+                    label |= bit << (n_mod - 1 - b);
+                }
             }
             sym[((size_t)f * xfec + j) * 2] = pts_re[label];
             sym[((size_t)f * xfec + j) * 2 + 1] = pts_im[label];

@@ -67,9 +67,12 @@ int orc_demap(const float* sym, int B, int xfec, int interleaved_len, int fec_le
               int kind, const float* pts_re, const float* pts_im, int n_points,
               const uint32_t* col_offset, float noise_var, float llr_gain, int16_t* out);
 
-/* Mapper: codeword N/8 bytes -> xfec complex symbols (re, im pairs). */
-int orc_map(const uint8_t* cw, int B, int cw_bytes, int xfec, int n_mod, const uint32_t* col_offset,
-            int stride, const float* pts_re, const float* pts_im, float* sym);
+/* Mapper: codeword N/8 bytes -> xfec complex symbols (re, im pairs).
+ * Symbols j < interleaved_len take label bits at col_offset[b] + j * stride,
+ * 0 at positions >= fec_len (stuffing); the rest (128APSK padding) carry
+ * the all-ones label (reference mapper.cc:28-62). */
+int orc_map(const uint8_t* cw, int B, int cw_bytes, int xfec, int interleaved_len, int fec_len, int n_mod,
+            const uint32_t* col_offset, int stride, const float* pts_re, const float* pts_im, float* sym);
 
 /* Known-answer hook: reference ldpc_make_bnl_update (message clamp, delta). */
 int orc_bnl_update(int raw_new, int old, int32_t* delta);

@@ -130,7 +130,7 @@ def demap(sym, xfec, interleaved_len, fec_len, n_mod, kind, pts, col, noise_var,
     return out
 
 
-def map_symbols(cw, xfec, n_mod, col, stride, pts):
+def map_symbols(cw, xfec, n_mod, col, stride, pts, interleaved_len=None, fec_len=None):
     cw = np.ascontiguousarray(cw, np.uint8)
     B = cw.shape[0]
     pts = np.asarray(pts, np.complex64)
@@ -138,7 +138,9 @@ def map_symbols(cw, xfec, n_mod, col, stride, pts):
     pim = np.ascontiguousarray(pts.imag, np.float32)
     col = np.ascontiguousarray(np.asarray(col, np.uint32).reshape(8))
     sym = np.zeros((B, xfec * 2), np.float32)
-    assert lib().orc_map(_p(cw, ctypes.c_uint8), B, cw.shape[1], xfec, n_mod, _p(col, ctypes.c_uint32),
+    il = xfec if interleaved_len is None else interleaved_len
+    fl = cw.shape[1] * 8 if fec_len is None else fec_len
+    assert lib().orc_map(_p(cw, ctypes.c_uint8), B, cw.shape[1], xfec, il, fl, n_mod, _p(col, ctypes.c_uint32),
                          stride, _p(pre, ctypes.c_float), _p(pim, ctypes.c_float),
                          _p(sym, ctypes.c_float)) == 0
     return sym

@@ -60,7 +60,7 @@ def test_invalid_arguments(built_lib):
     with pytest.raises(cs.CusatError):
         cs.code_info(7, 0)
     with pytest.raises(cs.CusatError):
-        cs.modcod_info(E.MOD_128APSK, E.RATE_135_180, E.FECFRAME_NORMAL)
+        cs.modcod_info(8, E.RATE_135_180, E.FECFRAME_NORMAL)
 
 
 @pytest.mark.parametrize("fs,r", [(0, 4), (0, 0), (0, 10), (0, 32), (1, 3), (1, 8), (0, 5)])
@@ -75,7 +75,8 @@ def test_product_encoder_matches_oracle(fs, r, built_lib):
     assert all(O.syndrome_ok(fs, r, l) for l in llr)
 
 
-@pytest.mark.parametrize("name", ["qpsk1/2", "8psk3/5", "16apsk2/3", "32apsk3/4", "64apsk32/45", "8apsk5/9"])
+@pytest.mark.parametrize("name", ["qpsk1/2", "8psk3/5", "16apsk2/3", "32apsk3/4", "64apsk32/45", "8apsk5/9",
+                                  "128apsk3/4", "256apsk3/4", "256apsk2/3"])
 def test_product_mapper_matches_oracle(name, built_lib):
     _, mod, r, *_ = E.find_modcod(name)
     fs = 0
@@ -86,8 +87,14 @@ def test_product_mapper_matches_oracle(name, built_lib):
     sym = cs.map_frames(mod, r, fs, cw)
     col = mi["col_offset"] if mod != E.MOD_QPSK else np.array([0, 1, 0, 0, 0, 0, 0, 0], np.uint32)
     stride = 2 if mod == E.MOD_QPSK else 1
-    ref_sym = O.map_symbols(cw, mi["xfecframe_len"], mi["n_mod"], col, stride, mi["points"])
+    ref_sym = O.map_symbols(cw, mi["xfecframe_len"], mi["n_mod"], col, stride, mi["points"],
+                            mi["interleaved_len"], mi["fecframe_len"])
     assert (sym == ref_sym).all()
+    if mod == E.MOD_128APSK:
+        # 6 stuffing bits, 12 padding symbols on the all-ones label (mapper.cc:28-62)
+        assert mi["interleaved_len"] == 9258 and mi["xfecframe_len"] == 9270
+        pad = sym[:, 2 * 9258:].reshape(2, 12, 2)
+        assert (pad[..., 0] == mi["points"][127].real).all() and (pad[..., 1] == mi["points"][127].imag).all()
 
 
 def test_interleaver_known_answers(built_lib):
@@ -127,6 +134,7 @@ def test_constellation_known_answers(built_lib):
     assert rings(E.MOD_16APSK, E.RATE_3_4) == 2 and rings(E.MOD_16APSK, E.RATE_90_180) == 2
     assert rings(E.MOD_32APSK, E.RATE_3_4) == 3 and rings(E.MOD_32APSK, E.RATE_128_180) == 4
     assert rings(E.MOD_64APSK, E.RATE_132_180) == 4
+    assert rings(E.MOD_128APSK, E.RATE_135_180) == 6 and rings(E.MOD_256APSK, E.RATE_135_180) == 8
     c = cs.modcod_info(E.MOD_16APSK, E.RATE_3_4, 0)["points"]
     assert abs(abs(c[0]) / abs(c[12]) - 2.85) < 1e-5
     for r, g1, g2 in [(6, 2.84, 5.27), (7, 2.72, 4.87), (8, 2.64, 4.64), (9, 2.54, 4.33), (10, 2.53, 4.30)]:

@@ -211,3 +211,26 @@ def test_single_code_objects_created_later_leave_the_batch_launchable(mixed):
     b.launch(frames, torch.cuda.current_stream())
     torch.cuda.synchronize()
     _check(bufs, ref)
+
+
+def test_mixed_batch_with_128_and_256_points(cuda):
+    """128APSK (9258 of 9270 symbols carry bits, 6 stuffing bits) and the
+    ring and coordinate 256APSK constellations in one mixed batch with 8PSK:
+    per frame the same results as single-MODCOD launches."""
+    torch = cuda
+    rng = np.random.default_rng(17)
+    per = []
+    for name, cnt in [("128apsk3/4", 3), ("256apsk32/45", 2), ("256apsk2/3", 2), ("8psk3/5", 2)]:
+        thr = E.find_modcod(name)[5]
+        msg, sym, n0, gain = traffic.modcod_frames(name, NORMAL, cnt, thr + 0.5, rng)
+        per.append((name, NORMAL, sym, [n0] * cnt, [gain] * cnt))
+    T = 30
+    ref = _single(per, T, torch)
+    assert all((r[1] >= 0).any() for r in ref)
+    order = [(m, i) for m, p in enumerate(per) for i in range(len(p[2]))]
+    order = [order[k] for k in rng.permutation(len(order))]
+    b = cs.batch(_modcod_triples(per), max_trials=T, max_frames=16)
+    bufs, frames = _buffers(per, order, torch)
+    b.launch(frames, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    _check(bufs, ref)

@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 NORMAL, SHORT = E.FECFRAME_NORMAL, E.FECFRAME_SHORT
 CASES = [("qpsk1/2", SHORT), ("qpsk1/4", NORMAL), ("8psk3/5", NORMAL), ("8psk3/5", SHORT), ("16apsk3/4", NORMAL),
-         ("32apsk4/5", NORMAL), ("64apsk32/45", NORMAL), ("8psk9/10", NORMAL), ("16apsk2/3", SHORT)]
+         ("32apsk4/5", NORMAL), ("64apsk32/45", NORMAL), ("8psk9/10", NORMAL), ("16apsk2/3", SHORT),
+         ("128apsk3/4", NORMAL), ("256apsk2/3", NORMAL), ("256apsk29/45", NORMAL)]
 
 
 @pytest.mark.parametrize("name,fs", CASES)

@@ -159,7 +159,8 @@ def test_batch_edges_and_errors(cuda):
 
 
 MODCOD_CASES = ["qpsk1/2", "qpsk3/4", "8psk3/5", "8psk9/10", "16apsk2/3", "16apsk5/6", "32apsk3/4",
-                "32apsk9/10", "64apsk32/45", "16apsk1/2l", "32apsk2/3l", "8apsk5/9"]
+                "32apsk9/10", "64apsk32/45", "16apsk1/2l", "32apsk2/3l", "8apsk5/9", "128apsk3/4", "128apsk7/9",
+                "256apsk3/4", "256apsk2/3", "256apsk11/15"]
 
 
 @pytest.mark.parametrize("name", MODCOD_CASES)
@@ -191,7 +192,8 @@ def test_demapper_bit_exact(cuda, name, fs):
 
 
 @pytest.mark.parametrize("name,fs", [("qpsk1/2", SHORT), ("8psk3/5", NORMAL), ("16apsk2/3", NORMAL),
-                                     ("32apsk3/4", SHORT), ("64apsk32/45", NORMAL)])
+                                     ("32apsk3/4", SHORT), ("64apsk32/45", NORMAL), ("128apsk7/9", NORMAL),
+                                     ("256apsk32/45", NORMAL)])
 def test_fused_chain_matches_separate_and_oracle(cuda, name, fs):
     torch = cuda
     _, mod, rate, _, _, thr = E.find_modcod(name)
