@@ -821,6 +821,9 @@ def learned_main(args, torch, cs, rank, local_rank, world):
 CODES = [("qpsk1/4", 0), ("qpsk1/2", 1), ("qpsk1/2", 0), ("8psk3/5", 1), ("8psk3/5", 0), ("16apsk3/4", 1),
          ("qpsk3/4", 0), ("16apsk5/6", 1), ("8psk5/6", 0), ("8psk8/9", 1), ("8psk9/10", 0)]
 
+DEMAP_MODCODS = ["qpsk1/2", "8psk3/5", "8apsk5/9", "16apsk2/3", "32apsk3/4", "64apsk32/45", "128apsk3/4",
+                 "256apsk3/4", "256apsk2/3"]
+
 
 def codes_main(args, torch, cs, rank, local_rank, world):
     """One MODCOD per kernel class (circulant slots per layer x lanes): 256
@@ -855,6 +858,39 @@ def codes_main(args, torch, cs, rank, local_rank, world):
         rows[f"{name} {'short' if fs else 'normal'}"] = {
             "slots": ci["cmax"], "lanes": ci["lanes"], "launch_ms": ms, "gbit_s": B * ci["k_ldpc"] / ms / 1e6,
             "mean_iterations": it, "edge_iterations_per_ns": B * it * ci["edges"] / ms / 1e6}
+    # the demapper per constellation family, normal frames: the demap launch
+    # alone and the whole receive launch (demap + decode + BCH) on the same
+    # 256 frames, so the demap's share of the path shows
+    demap = {}
+    for name in DEMAP_MODCODS:
+        _, mod, rate, _, _, thr = find_modcod(name)
+        _, sym, n0, gain = traffic.modcod_frames(name, 0, B, thr + 0.5, np.random.default_rng(6))
+        ci = cs.code_info(0, rate)
+        dm = cs.demapper_cuda(mod, rate, 0, B)
+        rx = cs.rx_fec(mod, rate, 0, 50, B)
+        d = torch.from_numpy(sym).cuda()
+        llr = torch.zeros((B, dm.fecframe_len()), dtype=torch.int16, device="cuda")
+        h = torch.zeros((B, rx.k_bytes), dtype=torch.uint8, device="cuda")
+        t = torch.zeros(B, dtype=torch.int32, device="cuda")
+        g = dm.capped_llr_gain(gain)
+
+        def timed(fn):
+            for _ in range(args.warmup):
+                fn()
+            ts = []
+            for _ in range(max(args.steps, 3)):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                fn()
+                b.record(st)
+                st.synchronize()
+                ts.append(a.elapsed_time(b))
+            return float(np.median(ts))
+        dms = timed(lambda: dm.demap_launch(d, B, n0, g, llr, st))
+        rms = timed(lambda: rx.launch(d, B, n0, gain, h, t, None, st))
+        demap[name] = {"bits_per_symbol": dm.n_mod(), "symbols_per_frame": dm.xfecframe_len(), "demap_ms": dms,
+                       "msym_s": B * dm.xfecframe_len() / dms / 1e3, "receive_ms": rms,
+                       "receive_gbit_s": B * ci["k_ldpc"] / rms / 1e6, "demap_share": dms / rms}
     if rank != 0:
         return
     head = rows["8psk3/5 normal"]
@@ -863,7 +899,7 @@ def codes_main(args, torch, cs, rank, local_rank, world):
         "warmup": args.warmup, "ms_per_step": head["launch_ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded frames at threshold + 0.5 dB)",
         "config": {"workload": "one MODCOD per decoder kernel class, 256 frames, single launches (inputs in "
-                               "L2 for the short codes)", "codes": rows}}), flush=True)
+                               "L2 for the short codes)", "codes": rows, "demap": demap}}), flush=True)
 
 
 # (micro_batch, streams, decode budget: -1 = one frame per SM, 0 = unlimited,

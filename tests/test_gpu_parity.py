@@ -239,3 +239,27 @@ def test_bch_check_matches_oracle(cuda, fs, rate, B):
         ro, vo = O.bch_check(fs, rate, words)
         assert (valid.cpu().numpy() == vo).all()
         assert (rem.cpu().numpy() == ro).all()
+
+
+@pytest.mark.parametrize("name", ["64apsk32/45", "128apsk3/4", "256apsk3/4", "256apsk2/3"])
+@pytest.mark.parametrize("offset_db,gain", [(-12.0, None), (12.0, None), (0.0, 0.0), (0.0, 1e-30), (0.0, 3e38),
+                                            (0.0, 1e5)])
+def test_demapper_cutoff_extremes(cuda, name, offset_db, gain):
+    """The 64- to 256-point log-MAP demapper at the edges of its cutoff (a
+    term counts when (d - min) * gain / 4 < 16): far below threshold (most
+    terms inside), far above (almost none), and gains of 0, 1e-30, 3e38 and
+    1e5 all give the oracle's LLRs."""
+    torch = cuda
+    _, mod, rate, _, _, thr = E.find_modcod(name)
+    _, _, noisy, n0, g0 = frames(mod, rate, NORMAL, 2, thr + offset_db, seed=23)
+    g = g0 if gain is None else gain
+    dm = cs.demapper_cuda(mod, rate, NORMAL, 2)
+    d_sym = torch.from_numpy(noisy).cuda()
+    out = torch.zeros((2, dm.fecframe_len()), dtype=torch.int16, device="cuda")
+    dm.demap_launch(d_sym, 2, n0, g, out, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    mi = cs.modcod_info(mod, rate, NORMAL)
+    ref = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"], mi["kind"],
+                  mi["points"], mi["col_offset"], n0, g)
+    got = out.cpu().numpy()
+    assert (got == ref).all(), f"{np.count_nonzero(got != ref)} LLRs differ"
