@@ -43,6 +43,92 @@ void launch_demap_kind(const DevDemap& d, const float2* sym, int batch, float no
     }
 }
 
+// Log-MAP with 32 to 256 points on symbols grouped by position.  The lanes
+// of a warp that demap 32 unrelated symbols between them need nearly every
+// (point, bit) exp; lanes whose symbols lie close together need the same
+// few.  A block takes a chunk of kSortChunk symbols of one frame, counting-
+// sorts them in shared memory by their cell of a kSortGrid x kSortGrid grid
+// over [-kSortR, kSortR]^2 (clamped at the edges), and demaps them in that
+// order with the vote variant of demap_logmap: per symbol the same terms in
+// the same order, so the LLRs do not depend on the grouping.
+constexpr int kSortThreads = 256, kSortChunk = 2048, kSortGrid = 16;
+constexpr float kSortR = 1.75f;  // unit-energy APSK: outer rings below 1.6
+
+template <int NM>
+__global__ void __launch_bounds__(kSortThreads) demap_sorted_kernel(DevDemap d, const float2* __restrict__ sym,
+                                                                   int16_t* __restrict__ out, float llr_gain)
+{
+    __shared__ float2 pts[1 << NM];
+    __shared__ int cell[kSortGrid * kSortGrid];
+    __shared__ uint16_t order[kSortChunk];
+    __shared__ uint8_t key[kSortChunk];
+    const int tid = threadIdx.x;
+    for (int k = tid; k < (1 << NM); k += kSortThreads)
+        pts[k] = d.points[k];
+    for (int k = tid; k < kSortGrid * kSortGrid; k += kSortThreads)
+        cell[k] = 0;
+    __syncthreads();
+    const int c0 = blockIdx.x * kSortChunk;
+    const int n = min(kSortChunk, d.interleaved_len - c0);
+    const float2* fs = sym + (size_t)blockIdx.y * d.xfec + c0;
+    const float gs = kSortGrid / (2.0f * kSortR);
+    for (int p = tid; p < n; p += kSortThreads) {
+        const float2 v = fs[p];
+        // fminf/fmaxf map NaN to the edge cell
+        const int cx = (int)fminf(fmaxf((v.x + kSortR) * gs, 0.0f), kSortGrid - 1.0f);
+        const int cy = (int)fminf(fmaxf((v.y + kSortR) * gs, 0.0f), kSortGrid - 1.0f);
+        key[p] = (uint8_t)(cy * kSortGrid + cx);
+        atomicAdd(&cell[cy * kSortGrid + cx], 1);
+    }
+    __syncthreads();
+    if (tid < 32) {  // exclusive scan of the 256 cell counts: 8 per lane
+        int v[8], sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            v[k] = cell[tid * 8 + k];
+            sum += v[k];
+        }
+        int inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (tid >= o)
+                inc += y;
+        }
+        int run = inc - sum;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            cell[tid * 8 + k] = run;
+            run += v[k];
+        }
+    }
+    __syncthreads();
+    for (int p = tid; p < n; p += kSortThreads)
+        order[atomicAdd(&cell[key[p]], 1)] = (uint16_t)p;
+    __syncthreads();
+    int16_t* o = out + (size_t)blockIdx.y * d.fec_len;
+    for (int r = 0; r < kSortChunk / kSortThreads; r++) {
+        const int slot = r * kSortThreads + tid;
+        if (r * kSortThreads + (tid & ~31) >= n)
+            break;  // the whole warp is past the chunk's symbols
+        const bool valid = slot < n;
+        const int p = valid ? order[slot] : 0;
+        const float2 v = valid ? fs[p] : make_float2(0.0f, 0.0f);
+        demap_logmap<NM, true>(d, pts, v.x, v.y, c0 + p, llr_gain, o, valid);
+    }
+}
+
+template <int NM>
+void launch_demap_sorted(const DevDemap& d, const float2* sym, int batch, float llr_gain, int16_t* out,
+                         cudaStream_t stream)
+{
+    for (int f0 = 0; f0 < batch; f0 += 65535) {
+        dim3 grid((d.interleaved_len + kSortChunk - 1) / kSortChunk, batch - f0 < 65535 ? batch - f0 : 65535);
+        demap_sorted_kernel<NM><<<grid, kSortThreads, 0, stream>>>(d, sym + (size_t)f0 * d.xfec,
+                                                                  out + (size_t)f0 * d.fec_len, llr_gain);
+    }
+}
+
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream)
 {
@@ -58,13 +144,13 @@ int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var
     else if (d.n_mod == 4)
         launch_demap_kind<2, 4>(d, s, batch, noise_var, llr_gain, out, stream);
     else if (d.n_mod == 5)
-        launch_demap_kind<2, 5>(d, s, batch, noise_var, llr_gain, out, stream);
+        launch_demap_sorted<5>(d, s, batch, llr_gain, out, stream);
     else if (d.n_mod == 6)
-        launch_demap_kind<2, 6>(d, s, batch, noise_var, llr_gain, out, stream);
+        launch_demap_sorted<6>(d, s, batch, llr_gain, out, stream);
     else if (d.n_mod == 7)
-        launch_demap_kind<2, 7>(d, s, batch, noise_var, llr_gain, out, stream);
+        launch_demap_sorted<7>(d, s, batch, llr_gain, out, stream);
     else if (d.n_mod == 8)
-        launch_demap_kind<2, 8>(d, s, batch, noise_var, llr_gain, out, stream);
+        launch_demap_sorted<8>(d, s, batch, llr_gain, out, stream);
     else
         launch_demap_kind<2, 0>(d, s, batch, noise_var, llr_gain, out, stream);
     return (int)cudaGetLastError();

@@ -120,9 +120,14 @@ __device__ __forceinline__ void demap_8psk(const DevDemap& d, float re, float im
 // APSK: log-MAP over the points (pts in shared memory), NM bits per symbol
 // (0: d.n_mod at run time; a compile-time NM resolves every label-bit test
 // and bit loop, same arithmetic; the point loops are then unrolled by 16).
-template <int NM>
+// VOTE: a term's exp is evaluated only when some lane of the warp has that
+// (point, bit) inside its cutoff, and each lane adds only its own terms (the
+// same terms in the same order, so the LLRs are those without VOTE); all 32
+// lanes must call it, `valid` false for a lane without a symbol (it adds
+// nothing and stores nothing).
+template <int NM, bool VOTE = false>
 __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pts, float re, float im, int j,
-                                             float llr_gain, int16_t* out)
+                                             float llr_gain, int16_t* out, bool valid = true)
 {
     constexpr int MB = NM ? NM : 8;
     const int nm = NM ? NM : d.n_mod;
@@ -162,16 +167,26 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
 #pragma unroll
         for (int b = 0; b < MB; b++) {
             if (NM || b < nm) {
-                if (i & (1 << (nm - 1 - b))) {
-                    const float delta = __fmul_rn(__fsub_rn(dd, mn1[b]), scale);
-                    if (delta < 16.0f) s1[b] = __fadd_rn(s1[b], dm_exp_neg(delta));
-                } else {
-                    const float delta = __fmul_rn(__fsub_rn(dd, mn0[b]), scale);
-                    if (delta < 16.0f) s0[b] = __fadd_rn(s0[b], dm_exp_neg(delta));
+                const bool one = i & (1 << (nm - 1 - b));
+                const float delta = __fmul_rn(__fsub_rn(dd, one ? mn1[b] : mn0[b]), scale);
+                if (VOTE) {
+                    const bool in = valid && delta < 16.0f;
+                    if (__any_sync(0xffffffffu, in)) {
+                        const float e = dm_exp_neg(delta);
+                        if (in && one) s1[b] = __fadd_rn(s1[b], e);
+                        if (in && !one) s0[b] = __fadd_rn(s0[b], e);
+                    }
+                } else if (delta < 16.0f) {
+                    if (one)
+                        s1[b] = __fadd_rn(s1[b], dm_exp_neg(delta));
+                    else
+                        s0[b] = __fadd_rn(s0[b], dm_exp_neg(delta));
                 }
             }
         }
     }
+    if (!valid)
+        return;
     const float half_gain = __fmul_rn(llr_gain, 0.5f);
 #pragma unroll
     for (int b = 0; b < MB; b++) {
