@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--duration", type=float, default=0.25, help="serve: seconds of traffic per rate")
     ap.add_argument("--pipe", type=int, default=0,
                     help="single/short: chains whose consecutive batches overlap (0 = enough to fill the resident CTA slots, at least 2)")
+    ap.add_argument("--demap-modcods", default="",
+                    help="codes: comma-separated MODCOD names for the demapper table (default: one per family)")
     ap.add_argument("--learned", action="store_true",
                     help="mixed/serve: decode each MODCOD with its adopted learned weights where one exists")
     return ap.parse_args()
@@ -862,7 +864,7 @@ def codes_main(args, torch, cs, rank, local_rank, world):
     # alone and the whole receive launch (demap + decode + BCH) on the same
     # 256 frames, so the demap's share of the path shows
     demap = {}
-    for name in DEMAP_MODCODS:
+    for name in (args.demap_modcods.split(",") if args.demap_modcods else DEMAP_MODCODS):
         _, mod, rate, _, _, thr = find_modcod(name)
         _, sym, n0, gain = traffic.modcod_frames(name, 0, B, thr + 0.5, np.random.default_rng(6))
         ci = cs.code_info(0, rate)

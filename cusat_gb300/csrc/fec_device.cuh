@@ -117,9 +117,19 @@ __device__ __forceinline__ void demap_8psk(const DevDemap& d, float re, float im
     }
 }
 
+// Points per unrolled step of the log-MAP loops: the label bits below
+// log2 of it are compile-time constants, but every unrolled point carries
+// its bits' exps inline, and past a few KB of loop body the warps wait on
+// instruction fetch (ncu, 256APSK unrolled by 16: 9.9 of 15.9 cycles per
+// issue stalled on no instruction).  Measured best on GB300 (demap of 256
+// normal frames): 16 points for up to 16 points, 8 for 32 and 64, 4 for 128
+// and 256 (256APSK 4.25 -> 2.73 ms, 128APSK 2.08 -> 1.41 ms).
+__host__ __device__ constexpr int logmap_unroll(int nm) { return nm == 0 ? 1 : nm <= 4 ? 16 : nm <= 6 ? 8 : 4; }
+
 // APSK: log-MAP over the points (pts in shared memory), NM bits per symbol
 // (0: d.n_mod at run time; a compile-time NM resolves every label-bit test
-// and bit loop, same arithmetic; the point loops are then unrolled by 16).
+// and bit loop, same arithmetic; the point loops are then unrolled by
+// logmap_unroll(NM)).
 // VOTE: a term's exp is evaluated only when some lane of the warp has that
 // (point, bit) inside its cutoff, and each lane adds only its own terms (the
 // same terms in the same order, so the LLRs are those without VOTE); all 32
@@ -131,8 +141,7 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
 {
     constexpr int MB = NM ? NM : 8;
     const int nm = NM ? NM : d.n_mod;
-    // a specialised call has exactly 2^NM points (checked by its launcher):
-    // unrolled by 16, the label bits below bit 4 are compile-time constants
+    // a specialised call has exactly 2^NM points (checked by its launcher)
     const int np = NM ? (1 << NM) : d.n_points;
     float mn0[MB], mn1[MB], s0[MB], s1[MB];
 #pragma unroll
@@ -142,7 +151,7 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
         s0[b] = 0.0f;
         s1[b] = 0.0f;
     }
-#pragma unroll (NM ? 16 : 1)
+#pragma unroll (logmap_unroll(NM))
     for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
@@ -159,7 +168,7 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
         }
     }
     const float scale = __fmul_rn(llr_gain, 0.25f);
-#pragma unroll (NM ? 16 : 1)
+#pragma unroll (logmap_unroll(NM))
     for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);

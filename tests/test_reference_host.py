@@ -105,7 +105,8 @@ def test_message_update_against_reference():
 
 @pytest.mark.parametrize("mod,rate,fs", [(E.MOD_QPSK, E.RATE_1_2, 1), (E.MOD_8PSK, E.RATE_3_5, 0),
                                          (E.MOD_16APSK, E.RATE_3_4, 0), (E.MOD_32APSK, E.RATE_3_4, 0),
-                                         (E.MOD_64APSK, E.RATE_4_5, 0)])
+                                         (E.MOD_64APSK, E.RATE_4_5, 0), (E.MOD_128APSK, E.RATE_135_180, 0),
+                                         (E.MOD_256APSK, E.RATE_20_30, 0), (E.MOD_256APSK, E.RATE_116_180, 0)])
 def test_dd_snr_matches_reference(mod, rate, fs, built_lib):
     """Decision-directed SNR: product and oracle bit-exact with the
     reference's dd_snr.cc on noisy constellation points, every stride."""
