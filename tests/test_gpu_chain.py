@@ -311,6 +311,39 @@ def test_mixed_pool_equals_per_modcod_pool(cuda, monkeypatch, pattern):
     assert mix.total_error_count() == per.total_error_count() > 0
 
 
+def test_mixed_pool_with_128_and_256_points(cuda, monkeypatch):
+    """Normal frames of 8PSK 3/5, 128APSK 3/4 (9270-symbol XFECFRAMEs, pilot
+    SNR) and 256APSK 2/3 (coordinate-defined points) in random order: the
+    mixed pool returns the per-MODCOD pool's bytes, sizes and counters."""
+    monkeypatch.setenv("CUSAT_LDPC_INFLIGHT_CAP", "0")
+    mods = [12, 32, 41]
+    frames = {}
+    for idx in mods:
+        mm = E.modcod_by_index(idx)
+        frames[idx] = list(traffic(mm[1], mm[2], NORMAL, 20, mm[5] + 0.8, seed=200 + idx))
+    rng = np.random.default_rng(11)
+    order = list(rng.permutation([m for m in mods for _ in range(20)]))
+    used = {m: 0 for m in mods}
+    seq = []
+    for m in order:
+        seq.append((frames[m][used[m]], int(m)))
+        used[m] += 1
+    per = cs.rx_fec_pool(NORMAL, mods, 50, 32, 2, 4)
+    mix = cs.rx_fec_pool(NORMAL, mods, 50, 32, 2, 4, mixed=True, slot_frames=8)
+    assert per.chain(32).xfecframe_len == 9270
+    for p in (per, mix):
+        p.warmup_all()
+        for idx in mods:
+            p.update_snr(idx, E.modcod_by_index(idx)[5] + 0.8)
+    out_p, dfl_p = _run_pool(per, seq, warm=False)
+    out_m, dfl_m = _run_pool(mix, seq, warm=False)
+    assert len(dfl_p) > len(seq) // 2
+    assert out_m.size == out_p.size and (out_m == out_p).all() and dfl_m == dfl_p
+    for idx in mods:
+        assert mix.modcod_counters(idx) == per.modcod_counters(idx)
+    assert mix.total_error_count() == per.total_error_count() > 0
+
+
 def test_mixed_pool_stale_launch_and_reset(cuda):
     pool = cs.rx_fec_pool(SHORT, [4, 12], 50, 64, 2, 4, mixed=True, slot_frames=32)
     pool.warmup_all()
