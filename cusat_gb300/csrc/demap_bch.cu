@@ -50,7 +50,8 @@ void launch_demap_kind(const DevDemap& d, const float2* sym, int batch, float no
 // sorts them in shared memory by their cell of a kSortGrid x kSortGrid grid
 // over [-kSortR, kSortR]^2 (clamped at the edges), and demaps them in that
 // order with the vote variant of demap_logmap: per symbol the same terms in
-// the same order, so the LLRs do not depend on the grouping.
+// the same order, so the LLRs do not depend on the grouping.  Reference
+// cuda/demapper_kernel.cu:108-183 (the APSK branch).
 constexpr int kSortThreads = 256, kSortChunk = 2048, kSortGrid = 16;
 constexpr float kSortR = 1.8f;  // unit-energy APSK: outer rings up to 1.70 (256APSK 31/45)
 
