@@ -55,23 +55,21 @@ void launch_demap_kind(const DevDemap& d, const float2* sym, int batch, float no
 constexpr int kSortThreads = 256, kSortChunk = 2048, kSortGrid = 16;
 constexpr float kSortR = 1.8f;  // unit-energy APSK: outer rings up to 1.70 (256APSK 31/45)
 
-template <int NM>
-__global__ void __launch_bounds__(kSortThreads) demap_sorted_kernel(DevDemap d, const float2* __restrict__ sym,
-                                                                   int16_t* __restrict__ out, float llr_gain)
+static_assert(kSortThreads == kDemapThreads, "the grouped chunk routine serves both demap kernels");
+
+// Sorts the n <= CH symbols fs[0..n) of a chunk of one frame (frame positions
+// c0..c0+n) by grid cell and demaps them in that order; all kSortThreads
+// threads of the block call it, and it leaves cell / order / key free for
+// the next chunk.
+template <int NM, int CH>
+__device__ __forceinline__ void demap_chunk_grouped(const DevDemap& d, const float2* pts, const float2* fs, int n,
+                                                    int c0, float llr_gain, int16_t* o, int* cell, uint16_t* order,
+                                                    uint8_t* key)
 {
-    __shared__ float2 pts[1 << NM];
-    __shared__ int cell[kSortGrid * kSortGrid];
-    __shared__ uint16_t order[kSortChunk];
-    __shared__ uint8_t key[kSortChunk];
     const int tid = threadIdx.x;
-    for (int k = tid; k < (1 << NM); k += kSortThreads)
-        pts[k] = d.points[k];
     for (int k = tid; k < kSortGrid * kSortGrid; k += kSortThreads)
         cell[k] = 0;
     __syncthreads();
-    const int c0 = blockIdx.x * kSortChunk;
-    const int n = min(kSortChunk, d.interleaved_len - c0);
-    const float2* fs = sym + (size_t)blockIdx.y * d.xfec + c0;
     const float gs = kSortGrid / (2.0f * kSortR);
     for (int p = tid; p < n; p += kSortThreads) {
         const float2 v = fs[p];
@@ -91,9 +89,9 @@ __global__ void __launch_bounds__(kSortThreads) demap_sorted_kernel(DevDemap d, 
         }
         int inc = sum;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (tid >= o)
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, off);
+            if (tid >= off)
                 inc += y;
         }
         int run = inc - sum;
@@ -107,8 +105,7 @@ __global__ void __launch_bounds__(kSortThreads) demap_sorted_kernel(DevDemap d, 
     for (int p = tid; p < n; p += kSortThreads)
         order[atomicAdd(&cell[key[p]], 1)] = (uint16_t)p;
     __syncthreads();
-    int16_t* o = out + (size_t)blockIdx.y * d.fec_len;
-    for (int r = 0; r < kSortChunk / kSortThreads; r++) {
+    for (int r = 0; r < CH / kSortThreads; r++) {
         const int slot = r * kSortThreads + tid;
         if (r * kSortThreads + (tid & ~31) >= n)
             break;  // the whole warp is past the chunk's symbols
@@ -117,6 +114,24 @@ __global__ void __launch_bounds__(kSortThreads) demap_sorted_kernel(DevDemap d, 
         const float2 v = valid ? fs[p] : make_float2(0.0f, 0.0f);
         demap_logmap<NM, true>(d, pts, v.x, v.y, c0 + p, llr_gain, o, valid);
     }
+    __syncthreads();
+}
+
+template <int NM>
+__global__ void __launch_bounds__(kSortThreads) demap_sorted_kernel(DevDemap d, const float2* __restrict__ sym,
+                                                                   int16_t* __restrict__ out, float llr_gain)
+{
+    __shared__ float2 pts[1 << NM];
+    __shared__ int cell[kSortGrid * kSortGrid];
+    __shared__ uint16_t order[kSortChunk];
+    __shared__ uint8_t key[kSortChunk];
+    for (int k = threadIdx.x; k < (1 << NM); k += kSortThreads)
+        pts[k] = d.points[k];
+    __syncthreads();
+    const int c0 = blockIdx.x * kSortChunk;
+    demap_chunk_grouped<NM, kSortChunk>(d, pts, sym + (size_t)blockIdx.y * d.xfec + c0,
+                                        min(kSortChunk, d.interleaved_len - c0), c0, llr_gain,
+                                        out + (size_t)blockIdx.y * d.fec_len, cell, order, key);
 }
 
 template <int NM>
@@ -165,6 +180,9 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
 {
     __shared__ float2 pts[256];
     __shared__ DevDemap d;
+    __shared__ int cell[kSortGrid * kSortGrid];
+    __shared__ uint16_t order[kDemapThreads * kDemapSpan];
+    __shared__ uint8_t key[kDemapThreads * kDemapSpan];
     const DemapFrame fr = frames[blockIdx.y];
     if (threadIdx.x == 0)
         d = demaps[fr.modcod];
@@ -176,6 +194,20 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
     const bool full = d.n_points == 1 << d.n_mod;  // 2^n_mod points: the specialised log-MAP applies
     const int sel = d.kind == 2 ? 2 * 16 + (full && d.n_mod >= 4 && d.n_mod <= 8 ? d.n_mod : 0) : d.kind * 16;
     const int per_block = kDemapThreads * kDemapSpan;
+    if (sel >= 37 && sel <= 40) {
+        // 32 to 256 points: the block's chunks grouped by position, as in
+        // demap_sorted_kernel
+        for (int base = blockIdx.x * per_block; base < d.interleaved_len; base += gridDim.x * per_block) {
+            const int n = min(per_block, d.interleaved_len - base);
+            switch (sel) {
+            case 37: demap_chunk_grouped<5, kDemapThreads * kDemapSpan>(d, pts, fr.sym + base, n, base, fr.llr_gain, fr.out, cell, order, key); break;
+            case 38: demap_chunk_grouped<6, kDemapThreads * kDemapSpan>(d, pts, fr.sym + base, n, base, fr.llr_gain, fr.out, cell, order, key); break;
+            case 39: demap_chunk_grouped<7, kDemapThreads * kDemapSpan>(d, pts, fr.sym + base, n, base, fr.llr_gain, fr.out, cell, order, key); break;
+            default: demap_chunk_grouped<8, kDemapThreads * kDemapSpan>(d, pts, fr.sym + base, n, base, fr.llr_gain, fr.out, cell, order, key); break;
+            }
+        }
+        return;
+    }
     for (int j0 = blockIdx.x * per_block + threadIdx.x; j0 - (int)threadIdx.x < d.interleaved_len;
          j0 += gridDim.x * per_block) {
         switch (sel) {
@@ -187,10 +219,6 @@ __global__ void __launch_bounds__(kDemapThreads) demap_mixed_kernel(const DevDem
                 const int j = j0 + u * kDemapThreads;
                 switch (sel) {
                 case 36: demap_span<2, 4, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                case 37: demap_span<2, 5, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                case 38: demap_span<2, 6, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                case 39: demap_span<2, 7, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
-                case 40: demap_span<2, 8, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 default: demap_span<2, 0, 1>(d, pts, fr.sym, fr.out, j, kDemapThreads, fr.noise_var, fr.llr_gain); break;
                 }
             }
