@@ -18,7 +18,7 @@ Checks performed before anything is written:
     printed values are unit energy up to their four decimals; the product
     still renormalises them, as the reference does).
 
-Usage:  python3 cusat_gb300/tables/gen_apsk256.py [--ref /root/reference]
+Usage:  python3 cusat_gb300/tables/gen_apsk256.py [--ref /root/reference] [--out FILE]
 """
 import argparse
 import os
@@ -45,6 +45,7 @@ def parse(text, name):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--out", default=OUT)
     args = ap.parse_args()
     text = open(os.path.join(args.ref, "lib/cusat_dsp/modulation/apsk256_points.h")).read()
     out = ["/* Generated by cusat_gb300/tables/gen_apsk256.py -- do not edit.",
@@ -61,10 +62,10 @@ def main():
             out.append("    " + " ".join(f"{a}f, {b}f," for a, b in pts[k:k + 4]))
         out.append("};")
         out.append("")
-    os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    with open(OUT, "w") as f:
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    with open(args.out, "w") as f:
         f.write("\n".join(out))
-    print("wrote", os.path.normpath(OUT))
+    print("wrote", os.path.normpath(args.out))
 
 
 if __name__ == "__main__":

@@ -126,3 +126,21 @@ def test_dd_snr_matches_reference(mod, rate, fs, built_lib):
     bad = np.full(20, np.nan, np.float32)
     assert cs.dd_snr(mod, rate, fs, bad) == 0.0 == ref.ref_dd_snr(mod, rate, fs, ctypes.c_void_p(_p(bad)), 10, 1,
                                                                  1 if mod == E.MOD_QPSK else 0)
+
+
+def test_apsk256_coordinate_tables_regenerate(tmp_path):
+    """csrc/gen/apsk256_points.inc is exactly what tables/gen_apsk256.py makes
+    from the reference's modulation/apsk256_points.h (its checks included)."""
+    import importlib.util
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(root, "oracle", "build.py"))
+    build = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(build)
+    out = tmp_path / "apsk256_points.inc"
+    subprocess.run([sys.executable, os.path.join(root, "cusat_gb300", "tables", "gen_apsk256.py"),
+                    "--ref", build.REF, "--out", str(out)], check=True, capture_output=True)
+    committed = os.path.join(root, "cusat_gb300", "csrc", "gen", "apsk256_points.inc")
+    assert out.read_bytes() == open(committed, "rb").read()
