@@ -52,7 +52,7 @@ void launch_demap_kind(const DevDemap& d, const float2* sym, int batch, float no
 // order with the vote variant of demap_logmap: per symbol the same terms in
 // the same order, so the LLRs do not depend on the grouping.  Reference
 // cuda/demapper_kernel.cu:108-183 (the APSK branch).
-constexpr int kSortThreads = 256, kSortChunk = 2048, kSortGrid = 16;
+constexpr int kSortThreads = 256, kSortChunk = 1024, kSortGrid = 16;
 constexpr float kSortR = 1.8f;  // unit-energy APSK: outer rings up to 1.70 (256APSK 31/45)
 
 static_assert(kSortThreads == kDemapThreads, "the grouped chunk routine serves both demap kernels");
