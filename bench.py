@@ -836,6 +836,8 @@ def codes_main(args, torch, cs, rank, local_rank, world):
     from cusat_gb300.enums import find_modcod
     B, rows = 256, {}
     st = torch.cuda.current_stream()
+    clocks = Clocks(local_rank)
+    clocks.start()
     for name, fs in CODES:
         _, mod, rate, _, _, thr = find_modcod(name)
         _, sym, n0, gain = traffic.modcod_frames(name, fs, B, thr + 0.5, np.random.default_rng(5))
@@ -893,6 +895,7 @@ def codes_main(args, torch, cs, rank, local_rank, world):
         demap[name] = {"bits_per_symbol": dm.n_mod(), "symbols_per_frame": dm.xfecframe_len(), "demap_ms": dms,
                        "msym_s": B * dm.xfecframe_len() / dms / 1e3, "receive_ms": rms,
                        "receive_gbit_s": B * ci["k_ldpc"] / rms / 1e6, "demap_share": dms / rms}
+    clk = clocks.stop()
     if rank != 0:
         return
     head = rows["8psk3/5 normal"]
@@ -901,7 +904,7 @@ def codes_main(args, torch, cs, rank, local_rank, world):
         "warmup": args.warmup, "ms_per_step": head["launch_ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int16", "data": "synthetic (seeded frames at threshold + 0.5 dB)",
         "config": {"workload": "one MODCOD per decoder kernel class, 256 frames, single launches (inputs in "
-                               "L2 for the short codes)", "codes": rows, "demap": demap}}), flush=True)
+                               "L2 for the short codes)", "codes": rows, "demap": demap}, "clocks": clk}), flush=True)
 
 
 # (micro_batch, streams, decode budget: -1 = one frame per SM, 0 = unlimited,
