@@ -528,7 +528,9 @@ int cusat_code_info(int framesize, int rate, int32_t* out);
  * ldpc_encode.cc:6-13). */
 int cusat_gen_encode(int framesize, int rate, const uint8_t* msg, uint8_t* cw, int batch);
 /* Interleave + map codewords to xfecframe_len symbols (re, im) per frame
- * (reference mapper.cc:75-86, cuda/mapper_kernel.cu:22-51). */
+ * (reference mapper.cc:75-86, cuda/mapper_kernel.cu:22-51); 128APSK: 6
+ * stuffing bits of 0 ahead of the interleaver and 12 padding symbols on the
+ * all-ones label after it (mapper.cc:28-62). */
 int cusat_gen_map(int modulation, int rate, int framesize, const uint8_t* cw, int batch, float* sym);
 /* Constellation points (2 * n_points floats, by label), interleaver column
  * offsets (8) and out[0..5] = n_mod, n_points, fecframe_len, xfecframe_len,
