@@ -55,12 +55,69 @@ PIPE = 2            # chains (streams) whose consecutive batches overlap, at lea
 RESIDENT_CTAS = 456 # resident decoder CTAs on a GB300 (152 SMs x 3 for short QPSK 1/2 frames)
 
 
-def n_bufs_for(wl):
+class ProductGen:
+    """Traffic generation with this project's encoder and mapper (GPU arm)."""
+
+    def __init__(self):
+        import cusat_gb300 as cs
+        self.cs = cs
+
+    def code_info(self, fs, rate):
+        return self.cs.code_info(fs, rate)
+
+    def encode(self, fs, rate, msg):
+        return self.cs.encode_frames(fs, rate, msg)
+
+    def map(self, mod, rate, fs, cw):
+        return self.cs.map_frames(mod, rate, fs, cw)
+
+    def modcod_info(self, mod, rate, fs):
+        return self.cs.modcod_info(mod, rate, fs)
+
+
+class OracleGen:
+    """The same traffic from the oracle's BCH/LDPC encoder and mapper (the
+    reference arm loads no library of this project); bit-identical to
+    ProductGen's output (tests/test_bench_host.py)."""
+
+    def __init__(self):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib as O
+        self.O = O
+
+    def code_info(self, fs, rate):
+        ci = self.O.code_info(fs, rate)
+        return {"k_bch": ci["k_bch"], "n_bch": ci["n_bch"], "k_ldpc": ci["K"], "n_ldpc": ci["N"],
+                "edges": ci["links_total"]}
+
+    def encode(self, fs, rate, msg):
+        return self.O.ldpc_encode(fs, rate, self.O.bch_encode(fs, rate, msg))
+
+    def map(self, mod, rate, fs, cw):
+        mi = self.O.modcod(mod, rate, fs)
+        qpsk = mi["kind"] == 0
+        col = np.arange(8, dtype=np.uint32) if qpsk else mi["col_offset"]
+        return self.O.map_symbols(cw, mi["xfecframe_len"], mi["n_mod"], col, 2 if qpsk else 1, mi["points"],
+                                  mi["interleaved_len"], mi["fecframe_len"])
+
+    def modcod_info(self, mod, rate, fs):
+        return self.O.modcod(mod, rate, fs)
+
+
+def n_bufs_for(wl, gen):
     """Batches to cycle through so that the inputs exceed the L2."""
-    import cusat_gb300 as cs
-    mi = cs.modcod_info(wl["mod"], wl["rate"], wl["fs"])
+    mi = gen.modcod_info(wl["mod"], wl["rate"], wl["fs"])
     batch_bytes = wl["frames"] * mi["xfecframe_len"] * 8
     return max(N_BUFS, int(np.ceil(L2_BYTES / batch_bytes)))
+
+
+def single_config(wl, nb, batch_bytes):
+    """The workload's config dict, the same in both arms (nothing measured)."""
+    return {"workload": f"{wl['name']} ({wl['code']}), {wl['frames']} frames, Es/N0 {wl['esn0_db']} dB: demap + "
+                        f"deinterleave -> layered min-sum LDPC (max {wl['max_trials']} it) -> BCH check",
+            "frames": wl["frames"], "max_trials": wl["max_trials"], "esn0_db": wl["esn0_db"], "seed": wl["seed"],
+            "decoder": "plain offset min-sum",
+            "l2": f"inputs cycled over {nb} batches ({nb * batch_bytes / 1e6:.0f} MB > L2)"}
 
 
 def parse():
@@ -92,15 +149,15 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
-def make_traffic(wl, n_bufs):
-    """n_bufs noisy batches of the workload (same codewords, fresh noise)."""
-    import cusat_gb300 as cs
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
+def make_traffic(wl, n_bufs, gen=None):
+    """n_bufs noisy batches of the workload (same codewords, fresh noise),
+    encoded and mapped by gen (ProductGen by default)."""
+    gen = gen or ProductGen()
     rng = np.random.default_rng(wl["seed"])
-    ci = cs.code_info(wl["fs"], wl["rate"])
+    ci = gen.code_info(wl["fs"], wl["rate"])
     msg = rng.integers(0, 256, (wl["frames"], ci["k_bch"] // 8), dtype=np.uint8)
-    cw = cs.encode_frames(wl["fs"], wl["rate"], msg)
-    sym = cs.map_frames(wl["mod"], wl["rate"], wl["fs"], cw)
+    cw = gen.encode(wl["fs"], wl["rate"], msg)
+    sym = gen.map(wl["mod"], wl["rate"], wl["fs"], cw)
     es = float(np.mean(sym.astype(np.float64) ** 2) * 2)
     sym = (sym / np.float32(np.sqrt(es))).astype(np.float32)
     n0 = np.float32(1.0 / 10 ** (wl["esn0_db"] / 10.0))
@@ -163,16 +220,14 @@ class Clocks:
 
 
 def cpu_chain(wl, bufs, n0, gain, n_frames, threads):
-    """Oracle demap + decode + BCH check of the first n_frames of batch 0."""
+    """Oracle demap + decode + BCH check of the first n_frames of batch 0
+    (demap parameters and gain cap from the oracle's own restatement)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import cusat_gb300 as cs
     import oracle_lib as O
-    mi = cs.modcod_info(wl["mod"], wl["rate"], wl["fs"])
-    g = cs.capped_llr_gain(wl["mod"], wl["rate"], wl["fs"], gain)
+    mi = O.modcod(wl["mod"], wl["rate"], wl["fs"])
     sym = bufs[0][:n_frames]
     t0 = time.perf_counter()
-    llr = O.demap(sym, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"],
-                  mi["kind"], mi["points"], mi["col_offset"], n0, g)
+    llr = O.demap_modcod(sym, mi, n0, gain)
     hard, trials = O.ldpc_decode(wl["fs"], wl["rate"], llr, wl["max_trials"], nthreads=threads)
     O.bch_check(wl["fs"], wl["rate"], hard)
     return time.perf_counter() - t0, trials
@@ -191,10 +246,15 @@ def cpu_sample(wl, bufs, n0, gain, threads, seconds):
 
 
 def reference_arm(args, wl):
+    """The reference's algorithm on the host cores: the oracle (the reference
+    ships no CPU decoder), fed by the oracle's own encoder and mapper -- no
+    library of this project is loaded in this arm."""
     rank, _, world = dist_env()
     if rank != 0:
         return
-    ci, msg, bufs, n0, gain = make_traffic(wl, 1)
+    gen = OracleGen()
+    nb = n_bufs_for(wl, gen)
+    ci, msg, bufs, n0, gain = make_traffic(wl, 1, gen)
     threads = os.cpu_count() or 1
     n = args.cpu_sample or wl["frames"]
     for _ in range(args.warmup):
@@ -207,13 +267,11 @@ def reference_arm(args, wl):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
-            "data": f"synthetic (seeded BCH/LDPC-encoded {wl['mod_name']} frames, AWGN)",
-            "config": {"workload": f"{wl['name']}: CPU demap + layered min-sum decode (max "
-                                   f"{wl['max_trials']} it) + BCH check, {n} frames per step",
-                       "frames": n, "esn0_db": wl["esn0_db"], "max_trials": wl["max_trials"]},
+            "data": f"synthetic (seeded BCH/LDPC-encoded {wl['mod_name']} frames, AWGN at Es/N0 {wl['esn0_db']} dB)",
+            "config": single_config(wl, nb, bufs[0].nbytes),
             "cpu_baseline": {"value": value, "unit": "Gbit/s", "cores": threads, "kind": "port",
-                             "sample": f"{n} frames of the workload per step (the reference ships no "
-                                       f"CPU decoder; C restatement of its algorithm)"},
+                             "sample": f"{n} frames of the workload's first batch per step, demap + decode + BCH "
+                                       f"(the reference ships no CPU decoder: C restatement of its algorithm)"},
             "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -255,26 +313,37 @@ def main():
             torch.distributed.destroy_process_group()
         return
 
-    nb = n_bufs_for(wl)
-    ci, msg, bufs, n0, gain = make_traffic(wl, nb)
+    gen = ProductGen()
+    nb = n_bufs_for(wl, gen)
+    ci, msg, bufs, n0, gain = make_traffic(wl, nb, gen)
     B, T = wl["frames"], wl["max_trials"]
-    # two chains on two streams: consecutive batches overlap, so the SMs that
-    # finish one batch's last frames start on the next batch
-    # enough chains in flight that small batches (64 short frames) fill the
+    mod, rate, fs = wl["mod"], wl["rate"], wl["fs"]
+    # chains on their own streams: consecutive batches overlap, so the SMs
+    # that finish one batch's last frames start on the next batch; enough
+    # chains in flight that small batches (64 short frames) fill the
     # resident CTA slots
     pipe = args.pipe or min(8, max(PIPE, -(-RESIDENT_CTAS // B)))
-    rxs = [cs.rx_fec(wl["mod"], wl["rate"], wl["fs"], T, B) for _ in range(pipe)]
     streams = [torch.cuda.Stream() for _ in range(pipe)]
+    # value: symbols already in HBM, one rx_fec launch (demap -> decode ->
+    # BCH) per batch into device outputs
+    rxs = [cs.rx_fec(mod, rate, fs, T, B) for _ in range(pipe)]
     d_sym = [torch.from_numpy(b).cuda() for b in bufs]
-    h_sym = [torch.from_numpy(b).pin_memory() for b in bufs]
     k_bytes = rxs[0].k_bytes
     outs = [(torch.zeros((B, k_bytes), dtype=torch.uint8, device="cuda"),
              torch.zeros(B, dtype=torch.int32, device="cuda"),
              torch.zeros(B, dtype=torch.int32, device="cuda")) for _ in range(pipe)]
-    d_in = [torch.empty_like(d_sym[0]) for _ in range(pipe)]
-    h_out = [(torch.empty((B, k_bytes), dtype=torch.uint8).pin_memory(),
-              torch.empty(B, dtype=torch.int32).pin_memory(),
-              torch.empty(B, dtype=torch.int32).pin_memory()) for _ in range(pipe)]
+    # e2e: the reference's per-slot launch sequence (rx_fec_chain.cc:361-505)
+    # through the library's host-buffer entry points -- demap_batch_async
+    # from pinned host symbols (copy into the demapper + demap),
+    # decode_launch_async from the demapper's LLRs into mapped pinned
+    # outputs, check_async of those outputs into a mapped pinned flag
+    h_sym = [torch.from_numpy(b).pin_memory() for b in bufs]
+    dms = [cs.demapper_cuda(mod, rate, fs, B) for _ in range(pipe)]
+    decs = [cs.ldpc_decode_cuda(fs, rate, T, B) for _ in range(pipe)]
+    bcs = [cs.bch_check_cuda.for_code(fs, rate) for _ in range(pipe)]
+    h_out = [(torch.zeros((B, k_bytes), dtype=torch.uint8).pin_memory(),
+              torch.zeros(B, dtype=torch.int32).pin_memory(),
+              torch.zeros(B, dtype=torch.int32).pin_memory()) for _ in range(pipe)]
 
     def barrier():
         torch.cuda.synchronize()
@@ -285,15 +354,14 @@ def main():
     def step(i, e2e):
         k = i % pipe
         st = streams[k]
-        hard, trials, valid = outs[k]
-        with torch.cuda.stream(st):
-            if e2e:
-                d_in[k].copy_(h_sym[i % nb], non_blocking=True)
-                rxs[k].launch(d_in[k], B, n0, gain, hard, trials, valid, st)
-                for h, d in zip(h_out[k], outs[k]):
-                    h.copy_(d, non_blocking=True)
-            else:
-                rxs[k].launch(d_sym[i % nb], B, n0, gain, hard, trials, valid, st)
+        if e2e:
+            hard, trials, valid = h_out[k]
+            dms[k].demap_batch_async(h_sym[i % nb].numpy(), B, n0, gain, st)
+            decs[k].decode_launch_async(dms[k].soft_out_dev(), B, st, hard, trials)
+            bcs[k].check_async(hard, valid, B, st)
+        else:
+            hard, trials, valid = outs[k]
+            rxs[k].launch(d_sym[i % nb], B, n0, gain, hard, trials, valid, st)
 
     def timed(e2e):
         for i in range(args.warmup):
@@ -402,17 +470,16 @@ def main():
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16",
         "data": f"synthetic (seeded BCH/LDPC-encoded {wl['mod_name']} frames, AWGN at Es/N0 {wl['esn0_db']} dB)",
-        "config": {"workload": f"{wl['name']} ({wl['code']}), {B} frames, Es/N0 {wl['esn0_db']} dB: demap + "
-                               f"deinterleave -> layered min-sum LDPC (max {T} it) -> BCH check",
-                   "frames": B, "max_trials": T, "esn0_db": wl["esn0_db"], "decoder": "plain offset min-sum",
-                   "parallelism": f"replicas x{world}; {pipe} chains on {pipe} streams, consecutive batches "
-                                  f"overlap",
-                   "launch_ms": launch_ms,
-                   "l2": f"inputs cycled over {nb} batches ({nb * bufs[0].nbytes / 1e6:.0f} MB > L2)",
-                   "mean_iterations": float(np.mean(it)), "p99_iterations": float(np.percentile(it, 99)),
-                   "frames_failed": int(np.sum(it >= T))},
+        "config": single_config(wl, nb, bufs[0].nbytes),
+        "stats": {"parallelism": f"replicas x{world}; {pipe} chains on {pipe} streams, consecutive batches overlap",
+                  "launch_ms": launch_ms, "mean_iterations": float(np.mean(it)),
+                  "p99_iterations": float(np.percentile(it, 99)), "frames_failed": int(np.sum(it >= T))},
         "e2e": {"value": e2e, "unit": "Gbit/s", "h2d_bytes_per_step": int(bufs[0].nbytes),
-                "d2h_bytes_per_step": int(B * (k_bytes + 8))},
+                "d2h_bytes_per_step": int(B * (k_bytes + 8)),
+                "path": "per batch: demapper_cuda.demap_batch_async from pinned host symbols (H2D copy + demap), "
+                        "ldpc_decode_cuda.decode_launch_async into mapped pinned hard bits and counts, "
+                        "bch_check_cuda.check_async of them into a mapped pinned flag -- the reference's "
+                        "launch_slot_gpu sequence; results written to host memory inside the timed region"},
         "roofline": {"bound": "hbm", "kernel": "ldpc_layered_kernel (decoder)", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "algorithmic_bytes": dec_bytes, "launch_ms": dec_ms,
@@ -456,11 +523,11 @@ class MixedTraffic:
     """The mixed workload packed into flat buffers: per frame a symbol slice,
     a hard-decision slice, an iteration counter and a BCH flag."""
 
-    def __init__(self, cs, n_frames, seed):
+    def __init__(self, cs, n_frames, seed, gen=None):
         from cusat_gb300 import traffic
         self.table, self.frames = traffic.mixed_traffic(n_frames, seed, short_share=MIXED["short_share"],
-                                                        margin_db=MIXED["margin_db"])
-        self.geo = traffic.geometry(self.table)
+                                                        margin_db=MIXED["margin_db"], gen=gen)
+        self.geo = traffic.geometry(self.table, gen)
         self.modcods = [(mod, rate, fs) for _, mod, rate, fs in self.table]
         self.sym_off, self.hard_off = [], []
         so = ho = 0
@@ -491,7 +558,6 @@ def cpu_mixed(mt, n_sample, threads, max_trials):
     call per MODCOD (the oracle spreads a call's frames over the threads);
     returns (seconds, information bits)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import cusat_gb300 as cs
     import oracle_lib as O
     groups = {}
     for fr in mt.frames[:n_sample]:
@@ -500,23 +566,28 @@ def cpu_mixed(mt, n_sample, threads, max_trials):
     bits = 0
     for m, frs in groups.items():
         _, mod, rate, fs = mt.table[m]
-        mi = cs.modcod_info(mod, rate, fs)
-        g = cs.capped_llr_gain(mod, rate, fs, frs[0]["gain"])
         sym = np.stack([fr["sym"] for fr in frs])
-        llr = O.demap(sym, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"],
-                      mi["n_mod"], mi["kind"], mi["points"], mi["col_offset"], frs[0]["n0"], g)
+        llr = O.demap_modcod(sym, O.modcod(mod, rate, fs), frs[0]["n0"], frs[0]["gain"])
         hard, _ = O.ldpc_decode(fs, rate, llr, max_trials, nthreads=threads)
         O.bch_check(fs, rate, hard)
         bits += mt.geo[m][1] * len(frs)
     return time.perf_counter() - t0, bits
 
 
+def mixed_config(n, learned, sets, sym_bytes):
+    """The mixed workload's config dict, the same in both arms."""
+    return {"workload": "mixed: 1024 frames of 10 MODCODs (64APSK 32/45 for S2X 64APSK 2/3), 70% normal "
+                        "/ 30% short, demap -> decode (max 50 it) -> BCH, one CUDA graph replay "
+                        "per step (tuned grid and class order)",
+            "frames": n, "max_trials": MIXED["max_trials"], "seed": MIXED["seed"], "learned_weights": bool(learned),
+            "l2": f"inputs alternate over {sets} sets ({sets * sym_bytes / 1e6:.0f} MB > L2)"}
+
+
 def mixed_reference_arm(args):
     rank, _, _ = dist_env()
     if rank != 0:
         return
-    import cusat_gb300 as cs
-    mt = MixedTraffic(cs, MIXED["frames"], MIXED["seed"])
+    mt = MixedTraffic(None, MIXED["frames"], MIXED["seed"], OracleGen())
     threads = os.cpu_count() or 1
     n = args.cpu_sample or 128
     cpu_mixed(mt, 2, threads, MIXED["max_trials"])
@@ -530,11 +601,12 @@ def mixed_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16",
-        "data": "synthetic (seeded mixed-MODCOD frames, AWGN at threshold + 0.5 dB)",
-        "config": {"workload": f"mixed 10 MODCODs: CPU demap + decode + BCH, first {n} frames per step",
-                   "frames": n},
+        "data": "synthetic (seeded mixed-MODCOD frames from the oracle's encoder and mapper, AWGN at each "
+                "MODCOD's threshold + 0.5 dB)",
+        "config": mixed_config(len(mt.frames), args.learned, MIXED["sets"], mt.sym.nbytes),
         "cpu_baseline": {"value": value, "unit": "Gbit/s", "cores": threads, "kind": "port",
-                         "sample": f"first {n} frames of the 1024-frame mixed batch per step"},
+                         "sample": f"first {n} frames of the 1024-frame mixed batch per step, demap + decode + "
+                                   f"BCH through the C oracle (plain decoder)"},
         "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
         flush=True)
 
@@ -665,16 +737,13 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "int16",
         "data": "synthetic (seeded mixed-MODCOD frames from this project's encoder and mapper, AWGN at each "
                 "MODCOD's threshold + 0.5 dB)",
-        "config": {"workload": "mixed: 1024 frames of 10 MODCODs (64APSK 32/45 for S2X 64APSK 2/3), 70% normal "
-                               "/ 30% short, demap -> decode (max 50 it) -> BCH, one CUDA graph replay "
-                               "per step (tuned grid and class order)",
-                   "frames": n, "max_trials": T, "kernel_classes": n_classes, "learned_weights": bool(args.learned),
-                   "parallelism": f"replicas x{world}; {S} graphs on {S} streams, consecutive batches overlap",
-                   "l2": f"inputs alternate over {S} sets ({S * mt.sym.nbytes / 1e6:.0f} MB > L2)",
-                   "batch_latency_ms": {"p50": lat_ms, "p99": float(np.percentile(lat, 99))},
-                   "tune_ms": [z["tune_ms"] for z in sets],
-                   "mean_iterations": float(np.mean(it)), "frames_failed": int(np.sum(trials < 0)),
-                   "per_modcod": per},
+        "config": mixed_config(n, args.learned, S, mt.sym.nbytes),
+        "stats": {"kernel_classes": n_classes,
+                  "parallelism": f"replicas x{world}; {S} graphs on {S} streams, consecutive batches overlap",
+                  "batch_latency_ms": {"p50": lat_ms, "p99": float(np.percentile(lat, 99))},
+                  "tune_ms": [z["tune_ms"] for z in sets],
+                  "mean_iterations": float(np.mean(it)), "frames_failed": int(np.sum(trials < 0)),
+                  "per_modcod": per},
         "e2e": {"value": e2e, "unit": "Gbit/s", "h2d_bytes_per_step": int(mt.sym.nbytes),
                 "d2h_bytes_per_step": int(mt.hard_bytes + 8 * n)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -759,7 +828,7 @@ def learned_main(args, torch, cs, rank, local_rank, world):
     w = learned.load_weights(wl["modcod"], wl["fs"])
     if w is None:
         raise RuntimeError("no adopted weight file for " + wl["modcod"])
-    nb = n_bufs_for(wl)
+    nb = n_bufs_for(wl, ProductGen())
     ci, msg, bufs, n0, gain = make_traffic(wl, nb)
     B = wl["frames"]
     sent = [torch.from_numpy(cs.encode_frames(wl["fs"], wl["rate"], msg)[:, :ci["k_ldpc"] // 8]).cuda()]
@@ -948,7 +1017,7 @@ def chain_main(args, torch, cs, rank, local_rank, world):
     step = 256 frames; wall time from the first submit to the end of the final
     flush.  value = the best setting's info Gbit/s."""
     wl = dict(WORKLOAD)
-    _, _, bufs, n0, _ = make_traffic(wl, n_bufs_for(wl))
+    _, _, bufs, n0, _ = make_traffic(wl, n_bufs_for(wl, ProductGen()))
     frames = [f for b in bufs for f in b]
     ci = cs.code_info(wl["fs"], wl["rate"])
     rows = {}

@@ -177,6 +177,11 @@ class ldpc_decode_cuda:
         p, n, _keep = _weights_arg(weights)
         _capi.check(_capi.lib().cusat_ldpc_decoder_set_weights(self._h, p, n))
 
+    def set_max_ctas(self, max_ctas):
+        """Caps the persistent grid (0 = no cap): each CTA then decodes
+        several frames of a batch in turn."""
+        _capi.check(_capi.lib().cusat_ldpc_decoder_set_max_ctas(self._h, max_ctas))
+
     def results(self, batch_size):
         hard = np.zeros((batch_size, self._kb), np.uint8)
         trials = np.zeros(batch_size, np.int32)
@@ -374,6 +379,10 @@ class batch:
         """Learned weights for MODCOD index `modcod` of this batch, or None."""
         p, n, _keep = _weights_arg(weights)
         _capi.check(_capi.lib().cusat_batch_set_weights(self._h, modcod, p, n))
+
+    def set_max_ctas(self, max_ctas):
+        """Caps every class's persistent grid (0 = no cap)."""
+        _capi.check(_capi.lib().cusat_batch_set_max_ctas(self._h, max_ctas))
 
     @staticmethod
     def frames(modcod, noise_var, llr_gain, sym, hard, trials, bch_valid=None):

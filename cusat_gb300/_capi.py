@@ -21,6 +21,7 @@ _SIGS = {
     "cusat_ldpc_decoder_destroy": (None, [ctypes.c_void_p]),
     "cusat_ldpc_decoder_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
     "cusat_ldpc_decoder_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_ldpc_decoder_set_max_ctas": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cusat_ldpc_decode_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "cusat_ldpc_decode_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -95,6 +96,7 @@ _SIGS = {
     "cusat_batch_destroy": (None, [ctypes.c_void_p]),
     "cusat_batch_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
     "cusat_batch_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_batch_set_max_ctas": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cusat_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "cusat_batch_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),

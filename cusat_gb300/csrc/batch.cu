@@ -68,6 +68,9 @@ struct cusat_batch {
     int max_n = 0, max_len = 0;                 // largest code length, largest interleaved length
     std::vector<int> class_count, class_off;
     cudaEvent_t fork = nullptr;
+    cudaEvent_t last = nullptr;  // recorded after every launch and replay
+    bool launched = false;
+    int max_ctas = 0;            // test hook: cap on every class's persistent grid (0 = none)
     // captured sequence: its own device descriptors (written once at capture),
     // so that later launches with other frames leave it intact
     cudaGraphExec_t graph = nullptr;
@@ -111,6 +114,7 @@ void release(cusat_batch* b)
     if (b->g_bch) cudaFree(b->g_bch);
     if (b->g_demap) cudaFree(b->g_demap);
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->last) cudaEventDestroy(b->last);
     delete b;
 }
 
@@ -197,6 +201,8 @@ int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, c
         a.n_frames = cnt;
         int grid = std::max(1, (int)(c.grid_frac * c.grid_max + 0.5f));
         grid = std::min(grid, std::min(cnt, c.grid_max));
+        if (b->max_ctas > 0)
+            grid = std::min(grid, b->max_ctas);
         const int rc = cusat::launch_decoder(c.fn, a, grid, c.threads, c.stream);
         if (rc)
             return cuda_fail((cudaError_t)rc, "decoder launch");
@@ -206,6 +212,8 @@ int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, c
     const int rc = cusat::launch_bch_check_mixed(b->d_bch_codes, d_bch, n, s);
     if (rc)
         return cuda_fail((cudaError_t)rc, "BCH launch");
+    CU(cudaEventRecord(b->last, s), "cudaEventRecord(last launch)");
+    b->launched = true;
     return CUSAT_OK;
 }
 
@@ -282,6 +290,7 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
         c.threads = cusat::decoder_threads(c.lanes);
         memset(&c.proto, 0, sizeof(c.proto));
         c.proto.max_trials = max_trials;
+        c.proto.syn_period = cusat::syndrome_period();
         cusat::decoder_smem_layout(&c.proto, dims);
         if (!c.fn || c.proto.sm_total > optin) {
             rc = fail(CUSAT_ERR_UNSUPPORTED, "no decoder kernel fits this MODCOD");
@@ -350,6 +359,8 @@ int cusat_batch_create(const int32_t* modcods, int n_modcods, int max_trials, in
             e = cudaMemcpy(b->d_bch_codes, bch.data(), bch.size() * sizeof(cusat::BchDev), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
             e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&b->last, cudaEventDisableTiming);
         if (e != cudaSuccess)
             rc = cuda_fail(e, "batch buffers");
     }
@@ -380,16 +391,19 @@ int cusat_batch_set_weights(cusat_batch* b, int modcod, const int16_t* weights, 
         return fail(CUSAT_ERR_ARG, "unknown MODCOD index");
     ModcodObj& m = *b->modcods[modcod];
     cusat::DevCode dc = m.dp.code;
-    CU(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    // this batch's last launch or replay still reads the tables; other
+    // streams of the application are not waited for
+    int rc = wait_last_launch(b->last, b->launched);
+    if (rc)
+        return rc;
     if (weights) {
-        const int rc = m.weights.set(weights, n_iter, b->max_trials);
+        rc = m.weights.set(weights, n_iter, b->max_trials);
         if (rc)
             return rc;
         dc.weights = m.weights.d;
     }
     KernelClass& c = b->classes[m.cls];
-    CU(cudaMemcpy(c.d_codes + m.code_in_class, &dc, sizeof(dc), cudaMemcpyHostToDevice), "cudaMemcpy(code)");
-    return CUSAT_OK;
+    return m.weights.upload(c.d_codes + m.code_in_class, &dc, sizeof(dc));
 }
 
 }  // extern "C"
@@ -471,6 +485,16 @@ int cusat_batch_replay(cusat_batch* b, void* stream)
     if (!b || !b->graph)
         return fail(CUSAT_ERR_ARG, "no captured batch");
     CU(cudaGraphLaunch(b->graph, (cudaStream_t)stream), "cudaGraphLaunch");
+    CU(cudaEventRecord(b->last, (cudaStream_t)stream), "cudaEventRecord(last launch)");
+    b->launched = true;
+    return CUSAT_OK;
+}
+
+int cusat_batch_set_max_ctas(cusat_batch* b, int max_ctas)
+{
+    if (!b || max_ctas < 0)
+        return fail(CUSAT_ERR_ARG, "null batch or negative CTA cap");
+    b->max_ctas = max_ctas;
     return CUSAT_OK;
 }
 

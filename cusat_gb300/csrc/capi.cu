@@ -34,6 +34,9 @@ struct Engine {
     uint4* msg = nullptr;
     unsigned int* queue = nullptr;
     DevWeights weights;
+    int max_ctas = 0;                 // test hook: cap on the persistent grid (0 = none)
+    cudaEvent_t last = nullptr;       // recorded after every launch
+    bool launched = false;
 
     int set_weights(const int16_t* w, int n_iter)
     {
@@ -41,8 +44,11 @@ struct Engine {
             proto.code.weights = nullptr;
             return CUSAT_OK;
         }
-        CU(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
-        const int rc = weights.set(w, n_iter, max_trials);
+        // a launch of this object still running reads the old table
+        int rc = wait_last_launch(last, launched);
+        if (rc)
+            return rc;
+        rc = weights.set(w, n_iter, max_trials);
         if (rc)
             return rc;
         proto.code.weights = weights.d;
@@ -67,6 +73,7 @@ struct Engine {
         memset(&proto, 0, sizeof(proto));
         proto.code = dp.code;
         proto.max_trials = max_trials;
+        proto.syn_period = cusat::syndrome_period();
         cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, p->lanes));
         int optin = 0, sms = 0;
         CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
@@ -85,6 +92,7 @@ struct Engine {
         const size_t msg_bytes = (size_t)grid_max * p->R * p->msg_row;
         CU(cudaMalloc(&msg, msg_bytes), "cudaMalloc(messages)");
         CU(cudaMalloc(&queue, 256), "cudaMalloc(queue)");
+        CU(cudaEventCreateWithFlags(&last, cudaEventDisableTiming), "cudaEventCreate");
         CU(cudaMemset(queue, 0, 256), "cudaMemset(queue)");  // the kernel rearms it after each launch
         proto.msg = msg;
         proto.msg_stride = p->R * p->msg_row / 16;
@@ -95,10 +103,14 @@ struct Engine {
     int launch(cusat::DecodeArgs a, int batch, cudaStream_t stream)
     {
         a.n_frames = batch;
-        const int grid = batch < grid_max ? batch : grid_max;
+        int grid = batch < grid_max ? batch : grid_max;
+        if (max_ctas > 0 && grid > max_ctas)
+            grid = max_ctas;
         const int rc = cusat::launch_decoder(fn, a, grid, threads, stream);
         if (rc != 0)
             return cuda_fail((cudaError_t)rc, "decoder launch");
+        CU(cudaEventRecord(last, stream), "cudaEventRecord(last launch)");
+        launched = true;
         return CUSAT_OK;
     }
 
@@ -111,6 +123,9 @@ struct Engine {
         if (queue)
             cudaFree(queue);
         weights.release();
+        if (last)
+            cudaEventDestroy(last);
+        last = nullptr;
         dp.blob = nullptr;
         msg = nullptr;
         queue = nullptr;
@@ -201,6 +216,14 @@ int cusat_ldpc_decoder_set_weights(cusat_ldpc_decoder* d, const int16_t* weights
     if (!d)
         return fail(CUSAT_ERR_ARG, "null decoder");
     return d->eng.set_weights(weights, n_iter);
+}
+
+int cusat_ldpc_decoder_set_max_ctas(cusat_ldpc_decoder* d, int max_ctas)
+{
+    if (!d || max_ctas < 0)
+        return fail(CUSAT_ERR_ARG, "null decoder or negative CTA cap");
+    d->eng.max_ctas = max_ctas;
+    return CUSAT_OK;
 }
 
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* d, int32_t* out)

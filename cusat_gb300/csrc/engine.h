@@ -76,11 +76,24 @@ inline int weight_table(const int16_t* w, int n_iter, int rows, std::vector<int1
     return CUSAT_OK;
 }
 
-// Device weight table of one code; set() replaces it, clear() returns to the
-// plain decoder.  Callers make sure no launch that reads it is in flight.
+// Waits for the work an event marks, if it was ever recorded: replacing a
+// table waits for the owning object's last launch, not for the device.
+inline int wait_last_launch(cudaEvent_t ev, bool recorded)
+{
+    if (ev && recorded)
+        CU(cudaEventSynchronize(ev), "cudaEventSynchronize(last launch)");
+    return CUSAT_OK;
+}
+
+// Device weight table of one code ([max(1, max_trials)][32][2] int16, one
+// allocation made on the first set); set() replaces its contents.  Callers
+// first wait for their own last launch that reads it (wait_last_launch); the
+// copy runs on a private non-blocking stream, so other streams of the
+// application are not stalled.
 struct DevWeights {
     int16_t* d = nullptr;
     int rows = 0;
+    cudaStream_t up = nullptr;
 
     int set(const int16_t* w, int n_iter, int max_trials)
     {
@@ -88,21 +101,34 @@ struct DevWeights {
         int rc = weight_table(w, n_iter, max_trials, &tab);
         if (rc)
             return rc;
-        if (!d || rows * 64 < (int)tab.size()) {
-            if (d)
-                cudaFree(d);
-            d = nullptr;
+        if (!d) {
             CU(cudaMalloc(&d, tab.size() * sizeof(int16_t)), "cudaMalloc(weights)");
             rows = (int)tab.size() / 64;
         }
-        CU(cudaMemcpy(d, tab.data(), tab.size() * sizeof(int16_t), cudaMemcpyHostToDevice), "cudaMemcpy(weights)");
+        if (!up)
+            CU(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking), "cudaStreamCreate(weights)");
+        CU(cudaMemcpyAsync(d, tab.data(), tab.size() * sizeof(int16_t), cudaMemcpyHostToDevice, up),
+           "cudaMemcpyAsync(weights)");
+        CU(cudaStreamSynchronize(up), "cudaStreamSynchronize(weights)");
+        return CUSAT_OK;
+    }
+    // copies one host object to device memory on the private stream
+    int upload(void* dst, const void* src, size_t n)
+    {
+        if (!up)
+            CU(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking), "cudaStreamCreate(weights)");
+        CU(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, up), "cudaMemcpyAsync(code)");
+        CU(cudaStreamSynchronize(up), "cudaStreamSynchronize(code)");
         return CUSAT_OK;
     }
     void release()
     {
         if (d)
             cudaFree(d);
+        if (up)
+            cudaStreamDestroy(up);
         d = nullptr;
+        up = nullptr;
         rows = 0;
     }
 };

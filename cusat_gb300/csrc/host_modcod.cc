@@ -6,6 +6,7 @@
 // (lib/cusat_dsp/modulation/constellation.cc); every point is produced with
 // the same float/double arithmetic so that the points are bit-identical to
 // the reference's (checked against the reference host code in the tests).
+#include <stdlib.h>
 #include <math.h>
 
 #include <cmath>
@@ -537,7 +538,10 @@ bool build_modcod_demap(int mod, int rate, int framesize, ModcodDemap* d, std::s
             }
         d->dmax = dmax;
     }
-    d->llr_target = 320.0f;
+    // LLR target of the gain cap: 320, or CUSAT_DEMAP_LLR_TARGET when set
+    // (read at construction, as the reference does: demapper_kernel.cu:238-239)
+    const char* tgt = getenv("CUSAT_DEMAP_LLR_TARGET");
+    d->llr_target = tgt ? (float)atof(tgt) : 320.0f;
     return true;
 }
 

@@ -45,6 +45,10 @@ const void* select_decoder_kernel(int cmax, int lanes);
 void decoder_smem_layout(DecodeArgs* a, const SmemDims& d);
 SmemDims smem_dims_of(const DevCode& c, int lanes);
 int decoder_threads(int lanes);
+// Syndrome-check period of every decoder launch: CUSAT_LDPC_SYN_PERIOD when
+// it is a positive integer, else 1; read once per process, like the
+// reference (cuda/ldpc_decode_kernel.cu:1237-1241).
+int syndrome_period();
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
 
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,

@@ -1,4 +1,6 @@
 // Instantiations and launch helpers of the layered decoder kernel.
+#include <stdlib.h>
+
 #include "kernels.h"
 #include "ldpc_kernel.cuh"
 
@@ -30,6 +32,15 @@ const void* select_decoder_kernel(int cmax, int lanes)
 }
 
 int decoder_threads(int lanes) { return lanes * lane_threads(lanes); }
+
+int syndrome_period()
+{
+    static const int period = [] {
+        const char* e = getenv("CUSAT_LDPC_SYN_PERIOD");
+        return (e && atoi(e) > 0) ? atoi(e) : 1;
+    }();
+    return period;
+}
 
 void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
 {

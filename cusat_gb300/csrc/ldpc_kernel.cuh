@@ -38,7 +38,9 @@
 //
 // Syndrome.  The check before each iteration (reference :693-745) votes
 // after the first step's checks and then every 4 steps, stopping at the
-// first failing group.
+// first failing group.  DecodeArgs::syn_period > 1 checks only before every
+// syn_period-th iteration and at the cap (the reference's
+// CUSAT_LDPC_SYN_PERIOD, :1237-1241).
 #pragma once
 
 #include "fec_device.cuh"
@@ -60,6 +62,7 @@ struct DecodeArgs {
     const FrameDesc* frames;
     const int16_t* llr;      // single code: [n_frames][N] int16 LLRs
     int n_frames, max_trials;
+    int syn_period;          // syndrome before iterations t with t % syn_period == 0 (and at the cap); <= 1: every one
     uint8_t* hard;           // single code: [n_frames][K/8]
     int32_t* trials;         // single code: [n_frames]
     uint4* msg;              // [gridDim.x][msg_stride] scratch
@@ -368,6 +371,7 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
     const int j = tid - lane * LT;
     const bool active = j < kM;
     const int K = c.K, q = c.q, T = a.max_trials, n_steps = c.n_steps;
+    const int period = a.syn_period > 1 ? a.syn_period : 1;
     const int pty = 2 * K;         // byte offset of the parity APP
     const int spare = 2 * c.N;     // scratch slot for the absent parity edge
     uint4* msg_cta = a.msg + (size_t)blockIdx.x * (size_t)a.msg_stride;
@@ -390,7 +394,9 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
             else
                 load_row<RW>(cur, src, load && active && i0 >= 0);
         }
-        if (syndrome_ok<CMAX>(smem, t, K, q, n_steps, lane, j, active)) {
+        // periodic + final check (reference ldpc_decode_kernel.cu:693-694)
+        if ((period == 1 || trial % period == 0 || trial == T) &&
+            syndrome_ok<CMAX>(smem, t, K, q, n_steps, lane, j, active)) {
             result = T - trial;
             break;
         }

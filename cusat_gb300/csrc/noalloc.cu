@@ -18,16 +18,21 @@
 //
 // All calls on a device share that device's copy of these arrays: two calls
 // whose kernels overlap on the GPU (for instance on two streams) race on
-// them.  The first call on a device looks up the arrays' device addresses and
-// sets the kernel's shared-memory limit; make that first call before any
-// stream capture.  A call for a code other than the previous call's uploads
-// that code's tables (a copy, not an allocation).
+// them.  Every call looks up the arrays' device addresses on the current
+// device (cheap, and still right after cudaDeviceReset has reloaded the
+// module) and copies its code's tables into the table area ahead of the
+// decode, on the caller's stream: at most 64 KiB from a static host buffer,
+// a copy and not an allocation.  No host-side record says which code the
+// table area holds, so calls for different codes in a row on one stream are
+// always decoded with their own tables.  A call on a stream that is being
+// captured into a CUDA graph is refused (CUSAT_ERR_UNSUPPORTED) and enqueues
+// nothing: a recorded table copy would read the static host buffer when the
+// graph runs, by which time another call may have refilled it.
 #include <cuda_runtime.h>
 #include <string.h>
 
 #include <mutex>
 #include <string>
-#include <vector>
 
 #include "../../include/cusat_fec.h"
 #include "host.h"
@@ -38,23 +43,22 @@ namespace {
 
 constexpr size_t kNoallocMsgBytes = 24u << 20;
 constexpr size_t kNoallocPlanBytes = 64u << 10;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_msg[kNoallocMsgBytes];
 static __device__ __align__(256) unsigned char g_noalloc_plan[kNoallocPlanBytes];
 static __device__ __align__(256) unsigned int g_noalloc_queue[64];
 
+// Host staging of the tables of the call in progress (guarded by g_mu).
+static unsigned char g_plan_host[kNoallocPlanBytes];
+
 struct DeviceState {
-    bool ready = false;
     unsigned char* msg = nullptr;    // device address of g_noalloc_msg on this device
     unsigned char* plan = nullptr;   // ... of g_noalloc_plan
     unsigned int* queue = nullptr;   // ... of g_noalloc_queue
     int sms = 0, optin = 0;
-    int loaded_fs = -1, loaded_rate = -1;  // code whose tables are in the plan area
 };
 
 std::mutex g_mu;
-DeviceState g_dev[kMaxDevices];
 
 // errors are reported through cusat_last_error(), like every entry point
 int fail(int code, const std::string& msg)
@@ -69,7 +73,8 @@ int cuda_fail(cudaError_t e, const char* what)
     return CUSAT_ERR_CUDA;
 }
 
-// One-time per device (with that device current): the arrays' device addresses.
+// With the device current: the arrays' device addresses and its limits
+// (looked up on every call).
 int setup_device(int dev, DeviceState* st)
 {
     cudaError_t e = cudaGetSymbolAddress((void**)&st->msg, g_noalloc_msg);
@@ -86,7 +91,6 @@ int setup_device(int dev, DeviceState* st)
         e = cudaDeviceGetAttribute(&st->optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaDeviceGetAttribute");
-    st->ready = true;
     return CUSAT_OK;
 }
 
@@ -109,13 +113,17 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices)
-        return fail(CUSAT_ERR_UNSUPPORTED, "device index above the supported count");
     cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaStreamIsCapturing");
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(CUSAT_ERR_UNSUPPORTED, "cusat_ldpc_decode_noalloc cannot be recorded into a CUDA graph");
 
     std::lock_guard<std::mutex> lock(g_mu);
-    DeviceState& st = g_dev[dev];
-    if (!st.ready) {
+    DeviceState st;
+    {
         const int rc = setup_device(dev, &st);
         if (rc)
             return rc;
@@ -138,18 +146,15 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     const size_t per_cta = (size_t)p->R * p->msg_row;
     if (per_cta > kNoallocMsgBytes)
         return fail(CUSAT_ERR_ARG, "message rows of one frame exceed the 24 MiB message area");
-    if (st.loaded_fs != framesize || st.loaded_rate != rate) {
-        std::vector<unsigned char> h(total, 0);
-        for (auto& pt : parts)
-            if (pt.n)
-                memcpy(&h[pt.off], pt.src, pt.n);
-        // pageable source: the copy is staged before the call returns
-        e = cudaMemcpyAsync(st.plan, h.data(), total, cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaMemcpyAsync(tables)");
-        st.loaded_fs = framesize;
-        st.loaded_rate = rate;
-    }
+    memset(g_plan_host, 0, total);
+    for (auto& pt : parts)
+        if (pt.n)
+            memcpy(&g_plan_host[pt.off], pt.src, pt.n);
+    // pageable source: the driver has staged the bytes when the call returns,
+    // so the next call may refill g_plan_host
+    e = cudaMemcpyAsync(st.plan, g_plan_host, total, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpyAsync(tables)");
 
     cusat::DecodeArgs a;
     memset(&a, 0, sizeof(a));
@@ -171,6 +176,7 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
     a.llr = soft_dev;
     a.n_frames = batch;
     a.max_trials = max_trials;
+    a.syn_period = cusat::syndrome_period();
     a.hard = hard_out;
     a.trials = trials_out;
     a.msg = (uint4*)st.msg;

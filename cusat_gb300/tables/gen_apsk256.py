@@ -18,7 +18,7 @@ Checks performed before anything is written:
     printed values are unit energy up to their four decimals; the product
     still renormalises them, as the reference does).
 
-Usage:  python3 cusat_gb300/tables/gen_apsk256.py [--ref /root/reference] [--out FILE]
+Usage:  python3 cusat_gb300/tables/gen_apsk256.py --ref REFERENCE_TREE (or CUSAT_REFERENCE_TREE set) [--out FILE]
 """
 import argparse
 import os
@@ -44,7 +44,8 @@ def parse(text, name):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CUSAT_REFERENCE_TREE"), required="CUSAT_REFERENCE_TREE" not in os.environ,
+                    help="root of the reference source tree")
     ap.add_argument("--out", default=OUT)
     args = ap.parse_args()
     text = open(os.path.join(args.ref, "lib/cusat_dsp/modulation/apsk256_points.h")).read()

@@ -22,7 +22,7 @@ Checks performed before anything is written:
   * the rate -> schedule registry (``ldpc_schedule_registry.h``) and the
     rate -> table factory (``ldpc_table_factory.cc``) agree on the table.
 
-Usage:  python3 cusat_gb300/tables/gen_tables.py [--ref /root/reference]
+Usage:  python3 cusat_gb300/tables/gen_tables.py --ref REFERENCE_TREE (or CUSAT_REFERENCE_TREE set)
 """
 import argparse
 import hashlib
@@ -118,7 +118,8 @@ def wrap(vals, per=20):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CUSAT_REFERENCE_TREE"), required="CUSAT_REFERENCE_TREE" not in os.environ,
+                    help="root of the reference source tree")
     ap.add_argument("--out", default=OUT)
     a = ap.parse_args()
     tdir = os.path.join(a.ref, "lib/cusat_dsp/ldpc_tables")

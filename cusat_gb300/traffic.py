@@ -31,17 +31,39 @@ def awgn(sym, esn0_db, rng):
     return (sym + sigma * rng.standard_normal(sym.shape, dtype=np.float32)).astype(np.float32), float(n0)
 
 
-def modcod_frames(name, fs, n, esn0_db, rng):
-    """n frames of one MODCOD: (messages, symbols [n, 2 xfec], N0, gain)."""
+class _PackageGen:
+    """Encoder and mapper of this package (the default generator)."""
+
+    @staticmethod
+    def code_info(fs, rate):
+        return code_info(fs, rate)
+
+    @staticmethod
+    def encode(fs, rate, msg):
+        return encode_frames(fs, rate, msg)
+
+    @staticmethod
+    def map(mod, rate, fs, cw):
+        return map_frames(mod, rate, fs, cw)
+
+    @staticmethod
+    def modcod_info(mod, rate, fs):
+        return modcod_info(mod, rate, fs)
+
+
+def modcod_frames(name, fs, n, esn0_db, rng, gen=None):
+    """n frames of one MODCOD: (messages, symbols [n, 2 xfec], N0, gain).
+    gen: an object with code_info/encode/map (default: this package's)."""
+    gen = gen or _PackageGen
     _, mod, rate, _, _, _ = find_modcod(name)
-    ci = code_info(fs, rate)
+    ci = gen.code_info(fs, rate)
     msg = rng.integers(0, 256, (n, ci["k_bch"] // 8), dtype=np.uint8)
-    sym = unit_energy(map_frames(mod, rate, fs, encode_frames(fs, rate, msg)))
+    sym = unit_energy(gen.map(mod, rate, fs, gen.encode(fs, rate, msg)))
     noisy, n0 = awgn(sym, esn0_db, rng)
     return msg, noisy, n0, min(4.0 / n0, 1000.0)
 
 
-def mixed_traffic(n_frames, seed, modcods=MIXED_MODCODS, short_share=0.3, margin_db=0.5):
+def mixed_traffic(n_frames, seed, modcods=MIXED_MODCODS, short_share=0.3, margin_db=0.5, gen=None):
     """Frames drawn uniformly over `modcods`, a share of them short (drawn
     among the short-capable ones), each at its threshold + margin (the
     reference's normal-frame thresholds, acm_config.h:54-115, also used for
@@ -62,18 +84,19 @@ def mixed_traffic(n_frames, seed, modcods=MIXED_MODCODS, short_share=0.3, margin
     for key in table:
         ids = [i for i, p in enumerate(picks) if p == key]
         thr = find_modcod(key[0])[5]
-        msg, noisy, n0, gain = modcod_frames(key[0], key[1], len(ids), thr + margin_db, rng)
+        msg, noisy, n0, gain = modcod_frames(key[0], key[1], len(ids), thr + margin_db, rng, gen)
         for k, i in enumerate(ids):
             frames[i] = {"modcod": index[key], "sym": noisy[k], "n0": n0, "gain": gain, "msg": msg[k]}
     out = [(name, find_modcod(name)[1], find_modcod(name)[2], fs) for name, fs in table]
     return out, frames
 
 
-def geometry(table):
+def geometry(table, gen=None):
     """Per table entry: xfecframe_len, k_ldpc, k_bch."""
+    gen = gen or _PackageGen
     geo = []
     for _, mod, rate, fs in table:
-        mi = modcod_info(mod, rate, fs)
-        ci = code_info(fs, rate)
+        mi = gen.modcod_info(mod, rate, fs)
+        ci = gen.code_info(fs, rate)
         geo.append((mi["xfecframe_len"], ci["k_ldpc"], ci["k_bch"]))
     return geo

@@ -68,9 +68,19 @@ int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* dec, int32_t* out);
  * min(max(m - 1, 0), 127), with m the smallest |extrinsic| of the other edges
  * and alpha in 64ths (0 = no scaling); iterations past n_iter reuse the last
  * row.  beta in 0..127, alpha in 0..255.  weights == NULL returns to the
- * plain decoder.  Waits for the device to go idle before replacing the
- * table. */
+ * plain decoder.  Waits for this decoder's last launch to finish (not for
+ * the device) before replacing the table, then copies it on a private
+ * non-blocking stream; launches captured in a CUDA graph are not waited
+ * for. */
 int cusat_ldpc_decoder_set_weights(cusat_ldpc_decoder* dec, const int16_t* weights, int n_iter);
+
+/* No counterpart in the reference, which launches one CTA per frame
+ * (ldpc_decode_kernel.cu:1198-1285).  Caps the CTAs of this decoder's
+ * persistent launches (0 = one per resident slot, at most one per frame).
+ * With fewer CTAs than frames each CTA decodes several frames in turn --
+ * the path every batch larger than the resident slots takes -- so small
+ * tests can hold that path against the oracle. */
+int cusat_ldpc_decoder_set_max_ctas(cusat_ldpc_decoder* dec, int max_ctas);
 
 /* Replaces ldpc_decode_cuda::decode_launch_async (ldpc_decode_kernel.cuh:51-64,
  * .cu:1324-1336): decodes `batch` frames of n_bits int16 LLRs read from
@@ -220,8 +230,14 @@ void cusat_batch_destroy(cusat_batch* b);
 /* out[0..3] = MODCODs, kernel classes, max_frames, max_trials */
 int cusat_batch_info(const cusat_batch* b, int32_t* out);
 /* Learned weights for one MODCOD of the batch (NULL: plain); takes effect
- * for later launches and for replays of an existing capture. */
+ * for later launches and for replays of an existing capture.  Waits for
+ * this batch's last launch or replay (not for the device) first. */
 int cusat_batch_set_weights(cusat_batch* b, int modcod, const int16_t* weights, int n_iter);
+/* Caps every kernel class's persistent grid at max_ctas CTAs (0 = no cap),
+ * so that CTAs decode several frames in turn and switch between the codes
+ * of their class -- what a large mixed batch does -- at sizes the oracle
+ * checks quickly.  Takes effect for later launches and captures. */
+int cusat_batch_set_max_ctas(cusat_batch* b, int max_ctas);
 /* Decodes n frames on `stream` (waits for the previous launch's descriptor
  * copies first; the frames' buffers must stay valid until completion).  One
  * launch (or replay) at a time per batch object: they share its LLR and
@@ -338,12 +354,13 @@ int cusat_nms_train_step(cusat_nms_trainer* tr, const int16_t* llr_dev, const ui
  * inside the library: 24 MiB of message rows (which bounds the CTAs used:
  * 60 for normal rate 3/5), 64 KiB of code tables, a frame counter.  They
  * exist on every device that loads the library until the process exits.
- * The first call on a device looks up their addresses and must come before
- * any stream capture; a call whose code differs from the previous call's
- * copies the new code's tables from host memory.  All calls on a device
- * share its arrays: calls whose kernels overlap on the GPU race.  Returns
- * CUSAT_ERR_ARG when a code's tables or one frame's message rows exceed the
- * arrays (no DVB-S2/S2X code does). */
+ * Every call looks up their addresses on the current device and copies its
+ * code's tables (at most 64 KiB, from a static host buffer) into the table
+ * area on `stream` ahead of the decode.  All calls on a device share its
+ * arrays: calls whose kernels overlap on the GPU race.  A call on a stream
+ * that is capturing a CUDA graph returns CUSAT_ERR_UNSUPPORTED and enqueues
+ * nothing.  Returns CUSAT_ERR_ARG when a code's tables or one frame's
+ * message rows exceed the arrays (no DVB-S2/S2X code does). */
 int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int16_t* soft_dev, int batch,
                               uint8_t* hard_out, int32_t* trials_out, void* stream);
 

@@ -295,7 +295,7 @@ static void pack_hard(const int16_t* app_d, int K, uint8_t* hard)
     }
 }
 
-static void decode_frame(const orc_code* c, orc_work* w, const int16_t* llr, int T,
+static void decode_frame(const orc_code* c, orc_work* w, const int16_t* llr, int T, int period,
                          const int16_t* weights, uint8_t* hard, int32_t* result)
 {
     const int K = c->K, R = c->R, q = c->q;
@@ -314,7 +314,8 @@ static void decode_frame(const orc_code* c, orc_work* w, const int16_t* llr, int
     int16_t x[64];
     int vn[64];
     for (int trial = 0; trial <= T; trial++) {
-        if (syndrome_ok(c, w->app_d, w->app_p)) {
+        /* periodic + final check (ldpc_decode_kernel.cu:693-694) */
+        if ((trial % period == 0 || trial == T) && syndrome_ok(c, w->app_d, w->app_p)) {
             pack_hard(w->app_d, K, hard);
             *result = T - trial;
             return;
@@ -396,8 +397,14 @@ static void decode_frame(const orc_code* c, orc_work* w, const int16_t* llr, int
 int orc_ldpc_decode(int framesize, int rate, const int16_t* llr, int B, int max_trials,
                     const int16_t* weights, uint8_t* hard, int32_t* trials, int nthreads)
 {
+    return orc_ldpc_decode_period(framesize, rate, llr, B, max_trials, 1, weights, hard, trials, nthreads);
+}
+
+int orc_ldpc_decode_period(int framesize, int rate, const int16_t* llr, int B, int max_trials, int syn_period,
+                           const int16_t* weights, uint8_t* hard, int32_t* trials, int nthreads)
+{
     const orc_code* c = get_code(framesize, rate);
-    if (!c || B < 0 || max_trials < 0)
+    if (!c || B < 0 || max_trials < 0 || syn_period < 1)
         return -1;
     if (nthreads <= 0)
         nthreads = 1;
@@ -418,7 +425,7 @@ int orc_ldpc_decode(int framesize, int rate, const int16_t* llr, int B, int max_
 #pragma omp for schedule(dynamic, 1)
 #endif
         for (int f = 0; f < B; f++)
-            decode_frame(c, &w, llr + (size_t)f * c->N, max_trials, weights,
+            decode_frame(c, &w, llr + (size_t)f * c->N, max_trials, syn_period, weights,
                          hard + (size_t)f * (c->K / 8), trials + f);
         free(w.app_d);
         free(w.app_p);
@@ -647,6 +654,45 @@ static inline int16_t llr_round(float v)
     v = rintf(v);
     v = fminf(fmaxf(v, -32768.0f), 32767.0f);
     return (int16_t)v;
+}
+
+/* Loudest-bit squared distance (demapper_kernel.cu:216-237).  The float
+ * sums are evaluated without contraction (the oracle is built with
+ * -ffp-contract=off), like the reference's host code. */
+float orc_demap_dmax(int kind, const float* pts_re, const float* pts_im, int n_points, int n_mod)
+{
+    if (kind == 0)
+        return 2.0f;
+    if (kind == 1)
+        return 4.0f;
+    float dmax = 0.0f;
+    for (int i = 0; i < n_points; i++) {
+        for (int b = 0; b < n_mod; b++) {
+            const int mask = 1 << (n_mod - 1 - b);
+            float dmin = 1e30f;
+            for (int k = 0; k < n_points; k++) {
+                if (((i ^ k) & mask) == 0)
+                    continue;
+                const float dr = pts_re[i] - pts_re[k];
+                const float di = pts_im[i] - pts_im[k];
+                const float d = dr * dr + di * di;
+                if (d < dmin)
+                    dmin = d;
+            }
+            if (dmin > dmax)
+                dmax = dmin;
+        }
+    }
+    return dmax;
+}
+
+/* demapper_cuda::capped_llr_gain (demapper_kernel.cu:283-291) */
+float orc_capped_llr_gain(float dmax, float llr_target, float llr_gain)
+{
+    if (llr_target <= 0.0f || dmax <= 0.0f)
+        return llr_gain;
+    const float cap = 2.0f * llr_target / dmax;
+    return llr_gain < cap ? llr_gain : cap;
 }
 
 int orc_demap(const float* sym, int B, int xfec, int interleaved_len, int fec_len, int n_mod,

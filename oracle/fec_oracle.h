@@ -45,6 +45,12 @@ int orc_code_info(int framesize, int rate, int32_t* out);
 int orc_ldpc_decode(int framesize, int rate, const int16_t* llr, int B, int max_trials,
                     const int16_t* weights, uint8_t* hard, int32_t* trials, int nthreads);
 
+/* Same, with the syndrome checked only before iterations t with
+ * t % syn_period == 0 and at t == max_trials (the reference's
+ * CUSAT_LDPC_SYN_PERIOD, ldpc_decode_kernel.cu:693-694,1237-1241). */
+int orc_ldpc_decode_period(int framesize, int rate, const int16_t* llr, int B, int max_trials, int syn_period,
+                           const int16_t* weights, uint8_t* hard, int32_t* trials, int nthreads);
+
 /* Syndrome of hard decisions from APP signs (test helper): 1 if every
  * parity check of the int16 LLR vector (< 0 = bit 1) is satisfied. */
 int orc_syndrome_ok(int framesize, int rate, const int16_t* llr);
@@ -66,6 +72,16 @@ int orc_bch_check(int framesize, int rate, const uint8_t* cw, uint8_t* rem, int3
 int orc_demap(const float* sym, int B, int xfec, int interleaved_len, int fec_len, int n_mod,
               int kind, const float* pts_re, const float* pts_im, int n_points,
               const uint32_t* col_offset, float noise_var, float llr_gain, int16_t* out);
+
+/* Demapper gain cap (reference cuda/demapper_kernel.cu:216-239, 283-291).
+ * dmax: "loudest bit" squared distance -- 2 for QPSK (kind 0), 4 for 8PSK
+ * (kind 1), else the largest over (point, bit) of the squared distance to
+ * the nearest point whose label differs in that bit.  The capped gain is
+ * min(llr_gain, 2 llr_target / dmax); llr_target <= 0 or dmax <= 0 leave
+ * llr_gain unchanged (the reference's target is 320 unless
+ * CUSAT_DEMAP_LLR_TARGET sets it). */
+float orc_demap_dmax(int kind, const float* pts_re, const float* pts_im, int n_points, int n_mod);
+float orc_capped_llr_gain(float dmax, float llr_target, float llr_gain);
 
 /* Mapper: codeword N/8 bytes -> xfec complex symbols (re, im pairs).
  * Symbols j < interleaved_len take label bits at col_offset[b] + j * stride,

@@ -8,7 +8,8 @@ on machines without the reference tree.
 Contents: FEC dimensions and BCH generators of every supported (frame size,
 rate); BCH codewords of seeded messages; interleaver column offsets and
 constellation points (as float32 bit patterns) of every MODCOD; the BB
-scrambler PRBS; GSE BBFRAMEs built by the reference and its data-field
+scrambler PRBS; the demapper's loudest-bit distance (dmax, which sets the
+LLR gain cap) of every MODCOD's reference points; GSE BBFRAMEs built by the reference and its data-field
 extraction of them; decision-directed SNR estimates of seeded symbols."""
 import ctypes
 import hashlib
@@ -78,9 +79,14 @@ def main():
             rows = np.zeros(1, np.uint32)
             ncol = ref.ref_interleaver(m[1], m[2], fs, p(col), p(rows))
             n = 1 << bits
+            # loudest-bit distance of the reference's points (the oracle's
+            # restatement of demapper_kernel.cu:216-237, float32 bits)
+            kind = 0 if m[1] == E.MOD_QPSK else 1 if m[1] == E.MOD_8PSK else 2
+            dmax = np.float32(O.lib().orc_demap_dmax(kind, p(re), p(im), n, bits))
             doc["modcods"].append({"name": m[3], "fs": fs, "bits": bits, "n_cols": int(ncol),
                                    "col": [int(v) for v in col], "re": re[:n].view(np.uint32).tolist(),
-                                   "im": im[:n].view(np.uint32).tolist()})
+                                   "im": im[:n].view(np.uint32).tolist(),
+                                   "dmax": int(dmax.view(np.uint32))})
     prbs = np.zeros(7274, np.uint8)
     ref.ref_bb_prbs(p(prbs), 7274)
     doc["prbs_head"] = prbs[:64].tobytes().hex()

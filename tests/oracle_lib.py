@@ -31,6 +31,9 @@ def lib():
         _lib.orc_log.restype = ctypes.c_float
         _lib.orc_log.argtypes = [ctypes.c_float]
         _lib.orc_dd_snr.restype = ctypes.c_float
+        _lib.orc_demap_dmax.restype = ctypes.c_float
+        _lib.orc_capped_llr_gain.restype = ctypes.c_float
+        _lib.orc_capped_llr_gain.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_float]
     return _lib
 
 
@@ -62,17 +65,70 @@ def code_info(fs, rate):
     return dict(zip(keys, (int(x) for x in out)))
 
 
-def ldpc_decode(fs, rate, llr, max_trials, weights=None, nthreads=8):
+def ldpc_decode(fs, rate, llr, max_trials, weights=None, nthreads=8, syn_period=1):
     info = code_info(fs, rate)
     llr = np.ascontiguousarray(llr, np.int16).reshape(-1, info["N"])
     B = llr.shape[0]
     hard = np.zeros((B, info["K"] // 8), np.uint8)
     trials = np.zeros(B, np.int32)
     w = None if weights is None else _p(np.ascontiguousarray(weights, np.int16), ctypes.c_int16)
-    rc = lib().orc_ldpc_decode(fs, rate, _p(llr, ctypes.c_int16), B, max_trials, w,
-                               _p(hard, ctypes.c_uint8), _p(trials, ctypes.c_int32), nthreads)
+    rc = lib().orc_ldpc_decode_period(fs, rate, _p(llr, ctypes.c_int16), B, max_trials, syn_period, w,
+                                      _p(hard, ctypes.c_uint8), _p(trials, ctypes.c_int32), nthreads)
     assert rc == 0
     return hard, trials
+
+
+_golden = None
+
+
+def golden():
+    """The reference's host-code answers (tests/golden/reference_host.json)."""
+    global _golden
+    if _golden is None:
+        import json
+        with open(os.path.join(ROOT, "tests", "golden", "reference_host.json")) as f:
+            _golden = json.load(f)
+    return _golden
+
+
+def modcod(mod, rate, fs, llr_target=320.0):
+    """Oracle-side demap parameters of a MODCOD, independent of the product:
+    the reference's constellation points and interleaver columns (golden
+    fixtures recorded from its host code), the frame geometry by the
+    reference's rules (demapper_kernel.cu:241-247: 128APSK stuffs 6 bits and
+    pads 12 symbols), the formula kind, and the loudest-bit distance dmax
+    computed by the oracle (demapper_kernel.cu:216-237)."""
+    from cusat_gb300 import enums as E
+    name = next(m[3] for m in E.MODCODS if (m[1], m[2]) == (mod, rate))
+    g = next(m for m in golden()["modcods"] if m["name"] == name and m["fs"] == fs)
+    bits = g["bits"]
+    n = 1 << bits
+    re = np.array(g["re"], np.uint32).view(np.float32)[:n].copy()
+    im = np.array(g["im"], np.uint32).view(np.float32)[:n].copy()
+    fec_len = 64800 if fs == 0 else 16200
+    if mod == E.MOD_128APSK:
+        il = (fec_len + 6) // bits
+        xfec = il + 12
+    else:
+        xfec = fec_len // bits
+        il = xfec
+    kind = 0 if mod == E.MOD_QPSK else 1 if mod == E.MOD_8PSK else 2
+    dmax = float(lib().orc_demap_dmax(kind, _p(re, ctypes.c_float), _p(im, ctypes.c_float), n, bits))
+    return {"n_mod": bits, "n_points": n, "fecframe_len": fec_len, "xfecframe_len": xfec,
+            "interleaved_len": il, "kind": kind, "points": (re + 1j * im).astype(np.complex64),
+            "col_offset": np.array(g["col"], np.uint32), "dmax": dmax, "llr_target": llr_target}
+
+
+def capped_llr_gain(mi, llr_gain):
+    """The oracle's gain cap for a modcod() description."""
+    return float(lib().orc_capped_llr_gain(mi["dmax"], mi["llr_target"], llr_gain))
+
+
+def demap_modcod(sym, mi, noise_var, llr_gain):
+    """Oracle demap of a modcod() description, with the oracle's own gain cap
+    applied to llr_gain (as the reference's callers do)."""
+    return demap(sym, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"], mi["kind"],
+                 mi["points"], mi["col_offset"], noise_var, capped_llr_gain(mi, llr_gain))
 
 
 def syndrome_ok(fs, rate, llr):

@@ -57,6 +57,37 @@ def test_constellations_and_interleavers(built_lib):
             assert mi["col_offset"].tolist() == m["col"]
 
 
+def test_llr_gain_cap_every_modcod(built_lib):
+    """The demapper's gain cap min(g, 2 * 320 / dmax) (reference
+    demapper_kernel.cu:216-239, 283-291): the oracle's dmax of the
+    reference's points equals the recorded one, and the product's cap equals
+    the oracle's for every MODCOD and frame size, bit for bit, over a range
+    of requested gains."""
+    for m in GOLD["modcods"]:
+        _, mod, rate, _, _, _ = E.find_modcod(m["name"])
+        mi = O.modcod(mod, rate, m["fs"])
+        assert np.float32(mi["dmax"]).view(np.uint32) == m["dmax"], m["name"]
+        for g in (1e9, 1000.0, 160.5, 15.92, 4.0, 0.5, 0.0):
+            want = O.capped_llr_gain(mi, g)
+            got = cs.capped_llr_gain(mod, rate, m["fs"], g)
+            assert np.float32(got).view(np.uint32) == np.float32(want).view(np.uint32), (m["name"], g, got, want)
+        if mod == E.MOD_8PSK:
+            assert O.capped_llr_gain(mi, 1e9) == 160.0  # 2 * 320 / 4
+
+
+def test_llr_target_knob(built_lib, monkeypatch):
+    """CUSAT_DEMAP_LLR_TARGET moves the cap as in the reference
+    (demapper_kernel.cu:238-239; <= 0 disables it)."""
+    mod, rate = E.MOD_16APSK, E.RATE_3_4
+    for tgt in ("100", "0"):
+        monkeypatch.setenv("CUSAT_DEMAP_LLR_TARGET", tgt)
+        mi = O.modcod(mod, rate, 0, llr_target=float(tgt))
+        want = O.capped_llr_gain(mi, 1e9)
+        assert cs.capped_llr_gain(mod, rate, 0, 1e9) == want
+    monkeypatch.delenv("CUSAT_DEMAP_LLR_TARGET")
+    assert cs.capped_llr_gain(mod, rate, 0, 1e9) == O.capped_llr_gain(O.modcod(mod, rate, 0), 1e9)
+
+
 def test_bb_scrambler_and_bbframes():
     prbs = O.bb_prbs(7274)
     assert prbs[:64].tobytes().hex() == GOLD["prbs_head"]

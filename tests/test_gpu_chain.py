@@ -44,7 +44,7 @@ class OracleChain:
 
     def __init__(self, mod, rate, fs, micro_batch, T):
         self.mod, self.rate, self.fs, self.mb, self.T = mod, rate, fs, micro_batch, T
-        self.mi = cs.modcod_info(mod, rate, fs)
+        self.mi = O.modcod(mod, rate, fs)
         self.kbch = cs.code_info(fs, rate)["k_bch"] // 8
         self.noise_var, self.llr_gain = np.float32(1.0), np.float32(4.0)
         self.skip, self.pending, self.pilot = 0, [], 0.0
@@ -80,7 +80,7 @@ class OracleChain:
         noisy = np.stack(self.pending)
         self.pending = []
         mi = self.mi
-        g = cs.capped_llr_gain(self.mod, self.rate, self.fs, float(self.llr_gain))
+        g = O.capped_llr_gain(mi, float(self.llr_gain))
         llr = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"],
                       mi["kind"], mi["points"], mi["col_offset"], float(self.noise_var), g)
         hard, trials = O.ldpc_decode(self.fs, self.rate, llr, self.T)

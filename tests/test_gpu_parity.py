@@ -2,8 +2,11 @@
 
 Decoder: hard decisions and iteration counts identical to the oracle on the
 same int16 LLRs; demapper: identical int16 LLRs; BCH: identical flags and
-remainders.  Sizes are those the oracle finishes in seconds; the full-size
-workloads are covered by size-independent properties in test_gpu_props.py.
+remainders.  The oracle side takes its demap parameters (points,
+interleaver columns, gain cap) from its own restatement and the reference's
+recorded host answers, never from the product.  The benchmark workloads at
+their full sizes, and CTAs that decode several frames in turn, are checked
+in test_gpu_bench_parity.py.
 """
 import numpy as np
 import pytest
@@ -19,10 +22,7 @@ NORMAL, SHORT = E.FECFRAME_NORMAL, E.FECFRAME_SHORT
 
 
 def oracle_llr(mod, rate, fs, noisy, n0, gain):
-    mi = cs.modcod_info(mod, rate, fs)
-    g = cs.capped_llr_gain(mod, rate, fs, gain)
-    return O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"],
-                   mi["kind"], mi["points"], mi["col_offset"], n0, g)
+    return O.demap_modcod(noisy, O.modcod(mod, rate, fs), n0, gain)
 
 
 def gpu_decode(torch, fs, rate, llr, T, max_batch=None):
@@ -258,7 +258,7 @@ def test_demapper_cutoff_extremes(cuda, name, offset_db, gain):
     out = torch.zeros((2, dm.fecframe_len()), dtype=torch.int16, device="cuda")
     dm.demap_launch(d_sym, 2, n0, g, out, torch.cuda.current_stream())
     torch.cuda.synchronize()
-    mi = cs.modcod_info(mod, rate, NORMAL)
+    mi = O.modcod(mod, rate, NORMAL)
     ref = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"], mi["kind"],
                   mi["points"], mi["col_offset"], n0, g)
     got = out.cpu().numpy()

@@ -14,10 +14,7 @@ SHORT, NORMAL = E.FECFRAME_SHORT, E.FECFRAME_NORMAL
 def _llr(mod, rate, fs, B, esn0, seed):
     import cusat_gb300 as cs
     _, cw, noisy, n0, gain = frames(mod, rate, fs, B, esn0, seed=seed)
-    mi = cs.modcod_info(mod, rate, fs)
-    g = cs.capped_llr_gain(mod, rate, fs, gain)
-    llr = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"],
-                  mi["kind"], mi["points"], mi["col_offset"], n0, g)
+    llr = O.demap_modcod(noisy, O.modcod(mod, rate, fs), n0, gain)
     return llr, cw
 
 

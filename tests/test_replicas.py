@@ -46,9 +46,7 @@ def _worker(rank, world, port, out_dir):
     fs, rate, mod = E.FECFRAME_SHORT, E.RATE_1_2, E.MOD_QPSK
     _, _, noisy, n0, gain = frames(mod, rate, fs, 6, 1.6, seed=11)
     import cusat_gb300 as cs
-    mi = cs.modcod_info(mod, rate, fs)
-    llr = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"], mi["kind"],
-                  mi["points"], mi["col_offset"], n0, cs.capped_llr_gain(mod, rate, fs, gain))
+    llr = O.demap_modcod(noisy, O.modcod(mod, rate, fs), n0, gain)
     a, b = R.shard(len(llr), rank, world)
     hard, trials = O.ldpc_decode(fs, rate, llr[a:b], 30, nthreads=1)
     t_max = R.reduce_timing([1.0 + rank, 5.0 - rank])
@@ -73,9 +71,7 @@ def test_two_ranks_over_gloo(tmp_path):
         assert list(r[k]["n_sum"]) == [6.0, 2.0]
     fs, rate, mod = E.FECFRAME_SHORT, E.RATE_1_2, E.MOD_QPSK
     _, _, noisy, n0, gain = frames(mod, rate, fs, 6, 1.6, seed=11)
-    mi = cs.modcod_info(mod, rate, fs)
-    llr = O.demap(noisy, mi["xfecframe_len"], mi["interleaved_len"], mi["fecframe_len"], mi["n_mod"], mi["kind"],
-                  mi["points"], mi["col_offset"], n0, cs.capped_llr_gain(mod, rate, fs, gain))
+    llr = O.demap_modcod(noisy, O.modcod(mod, rate, fs), n0, gain)
     hard, trials = O.ldpc_decode(fs, rate, llr, 30, nthreads=2)
     assert (np.concatenate([r[0]["hard"], r[1]["hard"]]) == hard).all()
     assert (np.concatenate([r[0]["trials"], r[1]["trials"]]) == trials).all()
