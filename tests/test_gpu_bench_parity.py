@@ -56,7 +56,7 @@ def test_bench_batches_match_oracle(cuda, which):
     torch = cuda
     bench = _bench()
     wl = dict(bench.WORKLOAD if which == "single" else bench.WORKLOAD_SHORT)
-    nb = bench.n_bufs_for(wl)
+    nb = bench.n_bufs_for(wl, bench.ProductGen())
     ci, msg, bufs, n0, gain = bench.make_traffic(wl, nb)
     B, T = wl["frames"], wl["max_trials"]
     mod, rate, fs = wl["mod"], wl["rate"], wl["fs"]
@@ -170,7 +170,9 @@ def test_few_ctas_decode_many_frames(cuda, fs, rate):
     cw = cs.encode_frames(fs, rate, msg)
     bits = np.unpackbits(cw, axis=1).astype(np.float32)
     R = ci["k_ldpc"] / ci["n_ldpc"]
-    ebn0 = 10 ** ((1.3 - 1.0 * (R < 0.5) + 1.5 * (R > 0.85)) / 10)
+    # past each code's waterfall (about 13-23 mean iterations) for the
+    # non-rail frames
+    ebn0 = 10 ** ((1.0 + (R >= 0.5) + 1.5 * (R > 0.7) + 1.0 * (R > 0.85)) / 10)
     sigma = np.sqrt(1 / (2 * R * ebn0))
     y = (1 - 2 * bits) + sigma * rng.standard_normal(bits.shape).astype(np.float32)
     llr = np.clip(np.rint(y * 2 / sigma ** 2 * 4), -32768, 32767).astype(np.int16)
@@ -190,4 +192,4 @@ def test_few_ctas_decode_many_frames(cuda, fs, rate):
         h, t = hard.cpu().numpy(), trials.cpu().numpy()
         bad = np.nonzero((t != to) | (h != ho).any(axis=1))[0]
         assert len(bad) == 0, f"launch {rep}: frames {bad[:8]} differ: trials gpu {t[bad[:8]]} oracle {to[bad[:8]]}"
-    assert (to >= 0).any()
+    assert (to >= 0).sum() >= B // 2 and (to < 0).any()
