@@ -49,7 +49,7 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
         *field = off;
         off = align16(off + bytes);
     };
-    take(&a->sm_dummy, 2 * kM * 2);  // +32767 region, then the junk region
+    take(&a->sm_dummy, 2 * kM * 2);  // +32640 region, then the junk region
     take(&a->sm_stage, kStageSets * kMaxStage * kM * 2);
     take(&a->sm_tab, d.q * d.cmax * 16);
     take(&a->sm_cnt, d.q);

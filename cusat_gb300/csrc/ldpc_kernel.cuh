@@ -20,12 +20,13 @@
 // Arithmetic.  The reference semantics (qsat16 extrinsic, offset min-sum
 // with beta 1, int8 clamp, saturating APP updates) are computed exactly.
 // When every channel LLR of the frame is within DevCode::fast_lim no
-// intermediate can leave int16 (|APP| <= |llr| + 127 (deg + 1)) and the
-// kernel runs the SAT = false path without clamps; otherwise the SAT = true
-// path evaluates every saturation.  Magnitudes are compared before the
-// offset: offset-then-clamp is monotone, so min1/min2 and the "is this edge
-// the minimum" test give the messages of the reference's finalp_oms_i16
-// (:242-275), ties included.
+// intermediate can leave int16 (|APP| <= |llr| + 127 dv) and the kernel
+// runs the packed path: two edges of a check row per 32-bit register as
+// int16 lanes (process_check_packed).  Otherwise one edge per instruction
+// with every saturation evaluated (process_check, SAT).  Magnitudes are
+// compared before the offset: offset-then-clamp is monotone, so min1/min2
+// and the "is this edge the minimum" test give the messages of the
+// reference's finalp_oms_i16 (:242-275), ties included.
 //
 // Checks of one step that share a variable node (a table row with two
 // accumulator addresses in one layer, or in both paired layers) are a data
@@ -332,6 +333,188 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
         __stcg(dst + w, make_uint4(wv[4 * w], wv[4 * w + 1], wv[4 * w + 2], wv[4 * w + 3]));
 }
 
+// ---------------------------------------------------------------------------
+// Packed 16-bit check rows (the saturation-free path).
+//
+// Two edges of a check row share one 32-bit register as a pair of int16
+// lanes (edge 2k in the low half, 2k + 1 in the high half): the extrinsic
+// values, the running min1/min2 and the message magnitudes and signs are
+// computed two edges per instruction with the packed 16-bit adds (FMA pipe)
+// and min/max/DPX ops (ALU pipe) of sm_90+, the work split about evenly
+// between the two pipes.  Exact: in this path every value is within int16
+// (|extrinsic| <= fast_lim + 127 (dv - 1), DevCode::fast_lim), so a packed
+// add never wraps where the result is used.
+//
+// Magnitudes are tracked bitwise complemented, nr = ~|x| = -|x| - 1 =
+// min(x - 1, ~x) (one DPX op given ~x), so min |x| is max nr.  With
+// r1 <= r2 the two smallest magnitudes clamped to 128 (a message is at most
+// 127: offset min-sum m = min(max(r - 1, 0), 127)), the message magnitude of
+// edge e is max(r1c + r2c + nr_e, r1c - 1, 0) -- r2c - 1 when |x_e| = r1
+// (the minimum edge; r1c - 1 as well when r1 = r2) and r1c - 1 when
+// |x_e| >= r2 -- one DPX op per pair.  With learned weights the two
+// magnitudes m1 <= m2 are computed per check and edge e takes m2 iff
+// |x_e| < r2.  The message sign is the sign of x_e times the product of all
+// signs (0 counts as +), as in the reference's finalp_oms_i16 (:242-275).
+// Message rows hold the negated messages -m, so that the extrinsic of the
+// next iteration is one packed add: x = APP + (-m).
+static __constant__ int c_pipe_k16 = 65536;  // IMAD operands the compiler cannot fold
+static __constant__ int c_pipe_k128 = 128;
+
+__device__ __forceinline__ uint32_t vadd2(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("add.s16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t vmin2(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("min.s16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t vmax2(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("max.s16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+// prmt with sign replication (bit 3 of a selector nibble)
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
+{
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+
+template <uint32_t F>
+__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t r;
+    asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(r) : "r"(a), "r"(b), "r"(c), "n"(F));
+    return r;
+}
+
+// Selector taking bytes s and s + 1 of a row word sign-extended into the two
+// int16 halves (s even); pad: the high half is 0.
+__host__ __device__ constexpr uint32_t pair_sel(int s, bool pad)
+{
+    return pad ? (uint32_t)(s | ((8 | s) << 4) | (4 << 8) | (4 << 12))
+               : (uint32_t)(s | ((8 | s) << 4) | ((s + 1) << 8) | ((8 | (s + 1)) << 12));
+}
+
+__device__ __forceinline__ int ldu16(const unsigned char* smem, int off)
+{
+    return *reinterpret_cast<const uint16_t*>(smem + off);
+}
+
+template <int CMAX, int RW, bool WTS>
+__device__ __forceinline__ void process_check_packed(const int16_t* wts, unsigned char* smem, const uint4* tb, int cnt,
+                                                     int j, int ps0, int ps1r, int ps1w, bool absent,
+                                                     const uint4 (&cur)[RW], uint4* dst, int trial)
+{
+    constexpr int NE = CMAX + 2;
+    constexpr int NP = (NE + 1) / 2;
+    constexpr bool kKeepAddr = CMAX <= 14;
+    const int one = c_pipe_one, neg = -one, k16 = c_pipe_k16;
+    const int j2 = j + j;
+    uint32_t x[NP];
+    int sa[kKeepAddr ? CMAX : 1];
+    // gather: x = APP + (-m_old) two edges at a time
+    {
+        const int a0 = ldu16(smem, ps0), a1 = ldu16(smem, ps1r);
+        x[0] = vadd2((uint32_t)madd(a1, k16, a0), prmt(cur[0].x, 0, pair_sel(0, false)));
+    }
+    int lo = 0;
+#pragma unroll
+    for (int c = 0; c < CMAX; c++) {
+        const int e = c + 2;
+        const uint4 w = tb[c];
+        const int ad = madd(rot720(j2, w.y, one), one, (int)w.x);
+        if (kKeepAddr)
+            sa[c] = madd((int)w.z, one, ad);
+        const int a = ldu16(smem, ad);
+        const uint32_t rw = word_of(cur[e >> 4], (e >> 2) & 3);
+        if ((e & 1) == 0) {
+            lo = a;
+            if (e == NE - 1)  // odd edge count: the high half is a pad that never wins a minimum
+                x[e >> 1] = vadd2((uint32_t)madd(32767, k16, lo), prmt(rw, 0, pair_sel(e & 3, true)));
+        } else {
+            x[e >> 1] = vadd2((uint32_t)madd(a, k16, lo), prmt(rw, 0, pair_sel((e - 1) & 3, false)));
+        }
+    }
+    // check node: max of ~|x| (= ~min |x|) and the runner-up, sign parity
+    uint32_t nr[NP];
+    uint32_t N1 = 0x80008000u, N2 = 0x80008000u, SX = 0;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        nr[k] = __viaddmin_s16x2(x[k], 0xffffffffu, (uint32_t)madd((int)x[k], neg, neg));  // min(x - 1, ~x) = ~|x|
+        const uint32_t t = vmin2(N1, nr[k]);
+        N2 = vmax2(N2, t);
+        N1 = vmax2(N1, nr[k]);
+        SX ^= x[k];
+    }
+    // both halves' results merged, replicated into both halves
+    const uint32_t N1s = prmt(N1, N1, 0x1032), N2s = prmt(N2, N2, 0x1032);
+    const uint32_t M1 = vmax2(N1, N1s);                              // ~r1
+    const uint32_t M2 = vmax2(vmin2(N1, N1s), vmax2(N2, N2s));        // ~r2
+    // message >= 0 iff sign(x_e) equals the parity of all signs T: Z has the
+    // sign bits set iff T = 0, so the sign bits of x ^ Z flag a message >= 0
+    const uint32_t w = SX ^ (uint32_t)madd((int)SX, k16, 0);
+    const uint32_t Z = lop3<0x0c>(prmt(w, 0, 0xbbbb), 0x80008000u, 0);   // ~a & b
+    uint32_t A, B, C;  // per-check constants of the magnitude rule
+    if (WTS) {
+        const int r1 = (int)(~M1 & 0xffffu), r2 = (int)(~M2 & 0xffffu);
+        const int deg = cnt + (absent ? 1 : 2);
+        const int16_t* wt = wts + ((size_t)trial * 32 + deg) * 2;
+        const int m1 = scaled_mag(r1, wt[0], wt[1]), m2 = scaled_mag(r2, wt[0], wt[1]);
+        A = (uint32_t)madd(m1, 0x10001, 0);
+        B = (uint32_t)madd(m2, 0x10001, 0);
+        C = vadd2((uint32_t)madd((int)M2, neg, neg), 0x00010001u);  // r2 + 1
+    } else {
+        const uint32_t R1c = vmin2((uint32_t)madd((int)M1, neg, neg), 0x00800080u);  // min(r1, 128)
+        const uint32_t R2c = vmin2((uint32_t)madd((int)M2, neg, neg), 0x00800080u);
+        A = vadd2(R1c, R2c);
+        B = __viaddmax_s16x2_relu(R1c, 0xffffffffu, 0u);  // max(r1c - 1, 0)
+        C = 0;
+    }
+    uint32_t nm[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        uint32_t mag;
+        if (WTS) {
+            const uint32_t lt = __viaddmin_s16x2_relu(C, nr[k], 0x00010001u);  // |x| < r2
+            mag = __viaddmin_s16x2(A, (uint32_t)madd((int)lt, c_pipe_k128, 0), B);
+        } else {
+            mag = __viaddmax_s16x2_relu(A, nr[k], B);
+        }
+        const uint32_t ns = prmt(x[k] ^ Z, 0, 0xbb99);  // 0xffff where the message is >= 0
+        const uint32_t P = vadd2(x[k], mag), Q = vadd2((uint32_t)madd((int)x[k], neg, neg), mag);
+        const uint32_t app = lop3<0xb1>(P, Q, ns);   // ns ? x + mag : ~(~x + mag) = x - mag
+        nm[k] = vadd2(mag, ns) ^ ns;                 // -message
+        const int lo_at = k == 0 ? ps0 : (kKeepAddr ? sa[2 * k - 2]
+                                                     : madd((int)tb[2 * k - 2].z, one,
+                                                            madd(rot720(j2, tb[2 * k - 2].y, one), one, (int)tb[2 * k - 2].x)));
+        sts16(smem, lo_at, (int)app);
+        if (2 * k + 1 < NE) {
+            const int hi_at = k == 0 ? ps1w : (kKeepAddr ? sa[2 * k - 1]
+                                                          : madd((int)tb[2 * k - 1].z, one,
+                                                                 madd(rot720(j2, tb[2 * k - 1].y, one), one, (int)tb[2 * k - 1].x)));
+            sts16(smem, hi_at, (int)__umulhi(app, (unsigned)k16));
+        }
+    }
+    // new message row: byte e = -message of edge e
+    uint32_t wv[RW * 4];
+#pragma unroll
+    for (int q = 0; q < RW * 4; q++)
+        wv[q] = 2 * q < NP ? prmt(nm[2 * q], 2 * q + 1 < NP ? nm[2 * q + 1] : 0u, 0x6420) : 0u;
+#pragma unroll
+    for (int q = 0; q < RW; q++)
+        __stcg(dst + q, make_uint4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]));
+}
+
 // Completion of step s's shared groups: thread j of each lane takes bit j of
 // the lane's items.  Plain path: APP + sum(row - APP); saturating path: the
 // rows hold deltas, sat16(APP + sum).
@@ -359,10 +542,14 @@ __device__ __forceinline__ void complete_groups(unsigned char* smem, const int16
     }
 }
 
-template <int CMAX, int LANES, bool SAT>
+// MODE 0: saturating arithmetic, one edge per instruction (frames with a
+// channel LLR beyond fast_lim); 1: packed pairs, plain offset min-sum;
+// 2: packed pairs with learned weights.
+template <int CMAX, int LANES, int MODE>
 __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned char* smem, const int16_t* stage,
                              const SmemCode& t, const Job& job)
 {
+    constexpr bool SAT = MODE == 0;
     constexpr int NE = CMAX + 2;
     constexpr int RW = (NE + 15) / 16;
     const int tid = threadIdx.x;
@@ -426,9 +613,18 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
                 if (i >= 0) {
                     const int ps0 = pty + 2 * (i * kM + j);
                     const bool absent = (i == 0 && j == 0);
-                    const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? spare : pty + 2 * ((q - 1) * kM + j - 1));
-                    process_check<CMAX, RW, SAT>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent, cur,
-                                                 msg_cta + ((size_t)i * kM + j) * RW, trial);
+                    uint4* dst = msg_cta + ((size_t)i * kM + j) * RW;
+                    if constexpr (SAT) {
+                        const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? spare : pty + 2 * ((q - 1) * kM + j - 1));
+                        process_check<CMAX, RW, true>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent,
+                                                      cur, dst, trial);
+                    } else {
+                        // the absent edge reads the +32640 region and writes the junk region
+                        const int ps1r = i > 0 ? ps0 - 2 * kM : (absent ? a.sm_dummy : pty + 2 * ((q - 1) * kM + j - 1));
+                        const int ps1w = absent ? a.sm_dummy + 2 * kM : ps1r;
+                        process_check_packed<CMAX, RW, MODE == 2>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0,
+                                                                  ps1r, ps1w, absent, cur, dst, trial);
+                    }
                 }
             }
             if (t.conf[s] == kConfMid) {
@@ -561,7 +757,11 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), min_ctas_per_sm(C
                         reinterpret_cast<const uint2*>(smem + a.sm_items)};
 
     for (int k = threadIdx.x; k < kM; k += blockDim.x)
-        dummy[k] = 32767;  // absent circulants read +32767: never a minimum, no sign
+        // absent edges read +32640: with a message of at most 127 subtracted
+        // their extrinsic stays in [32513, 32767] -- positive, above every
+        // real magnitude of the saturation-free path (<= fast_lim + 127 (dv - 1)
+        // = 32386) and above 127, so it never changes a message
+        dummy[k] = 32640;
     int loaded = -1;
     for (;;) {
         __syncthreads();
@@ -590,9 +790,11 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), min_ctas_per_sm(C
         }
         const int over = load_llr(c, app, job.llr);
         if (__syncthreads_or(over))
-            decode_frame<CMAX, LANES, true>(a, c, smem, stage, t, job);
+            decode_frame<CMAX, LANES, 0>(a, c, smem, stage, t, job);
+        else if (c.weights)
+            decode_frame<CMAX, LANES, 2>(a, c, smem, stage, t, job);
         else
-            decode_frame<CMAX, LANES, false>(a, c, smem, stage, t, job);
+            decode_frame<CMAX, LANES, 1>(a, c, smem, stage, t, job);
     }
     // The last CTA out rearms the counters for the next launch (no memset
     // before each launch or graph replay): every CTA has drawn its final
