@@ -742,6 +742,7 @@ def mixed_main(args, torch, cs, rank, local_rank, world):
                   "parallelism": f"replicas x{world}; {S} graphs on {S} streams, consecutive batches overlap",
                   "batch_latency_ms": {"p50": lat_ms, "p99": float(np.percentile(lat, 99))},
                   "tune_ms": [z["tune_ms"] for z in sets],
+                  "tuned": sets[0]["b"].tuned(),
                   "mean_iterations": float(np.mean(it)), "frames_failed": int(np.sum(trials < 0)),
                   "per_modcod": per},
         "e2e": {"value": e2e, "unit": "Gbit/s", "h2d_bytes_per_step": int(mt.sym.nbytes),

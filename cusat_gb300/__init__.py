@@ -406,6 +406,20 @@ class batch:
                                                  _stream(stream), ctypes.byref(best)))
         return best.value
 
+    def tuned(self):
+        """The tuned launch configuration: one dict per kernel class."""
+        out = np.zeros(5 * 64, np.int32)
+        solo = np.zeros(64, np.float32)
+        n = _capi.lib().cusat_batch_tuned(self._h, out.ctypes.data, solo.ctypes.data, 64)
+        _capi.check(min(n, 0))
+        res = []
+        for k in range(n):
+            cmax, lanes, frames, grid, pos = (int(v) for v in out[5 * k:5 * k + 5])
+            res.append({"slots": cmax, "lanes": lanes, "frames": frames, "ctas": grid,
+                        "frames_per_cta": frames / grid if grid else None, "order": pos,
+                        "solo_ms": float(solo[k])})
+        return res
+
     def capture(self, frames, stream):
         self._frames = frames
         _capi.check(_capi.lib().cusat_batch_capture(self._h, ctypes.addressof(frames), len(frames),

@@ -97,6 +97,7 @@ _SIGS = {
     "cusat_batch_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
     "cusat_batch_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "cusat_batch_set_max_ctas": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_batch_tuned": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "cusat_batch_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)]),

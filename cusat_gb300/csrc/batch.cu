@@ -44,8 +44,10 @@ struct KernelClass {
     unsigned int* queue = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    // tuned launch: fraction of grid_max (1.0 = every resident CTA slot)
-    float grid_frac = 1.0f;
+    // tuned launch: persistent CTAs of this class's decoder (0 = every
+    // resident slot), i.e. about count / grid frames per CTA
+    int grid = 0;
+    float tuned_ms = 0.0f;  // the class's decoder alone on its full grid, at the last tuning
 };
 
 }  // namespace
@@ -199,7 +201,7 @@ int enqueue(cusat_batch* b, int n, cudaStream_t s, cusat::FrameDesc* d_frames, c
         cusat::DecodeArgs a = c.proto;
         a.frames = d_frames + b->class_off[k];
         a.n_frames = cnt;
-        int grid = std::max(1, (int)(c.grid_frac * c.grid_max + 0.5f));
+        int grid = c.grid > 0 ? c.grid : c.grid_max;
         grid = std::min(grid, std::min(cnt, c.grid_max));
         if (b->max_ctas > 0)
             grid = std::min(grid, b->max_ctas);
@@ -508,65 +510,168 @@ int cusat_batch_tune(cusat_batch* b, const cusat_frame* frames, int n, int reps,
     if (rc)
         return rc;
     const int nc = (int)b->classes.size();
-    // work of a class ~ frames x edges; classes with more work launch first
-    std::vector<double> work(nc, 0.0);
-    for (int i = 0; i < n; i++) {
-        const ModcodObj& m = *b->modcods[frames[i].modcod];
-        work[m.cls] += m.plan->links_total;
-    }
-    double total = 0;
-    for (double w : work)
-        total += w;
-    std::vector<int> by_work(nc);
-    for (int k = 0; k < nc; k++)
-        by_work[k] = k;
-    std::sort(by_work.begin(), by_work.end(), [&](int x, int y) { return work[x] > work[y]; });
-    std::vector<int> by_work_rev(by_work.rbegin(), by_work.rend());
-    // candidates: (order, grid rule); grid rule 0 = every resident slot,
-    // 1 = slots in proportion to the class's share of the work
-    struct Cand { const std::vector<int>* order; int rule; };
-    const Cand cands[] = {{&by_work, 0}, {&by_work, 1}, {&by_work_rev, 0}, {&by_work_rev, 1}};
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0), "cudaEventCreate");
     CU(cudaEventCreate(&e1), "cudaEventCreate");
-    float best = 1e30f;
-    int best_i = 0;
-    for (int ci = 0; ci < 4; ci++) {
-        b->order = *cands[ci].order;
-        for (int k = 0; k < nc; k++)
-            b->classes[k].grid_frac =
-                cands[ci].rule == 0 ? 1.0f : (float)std::max(0.05, total > 0 ? work[k] / total : 1.0);
+    // mean time of reps launch sequences (one untimed first: caches, clocks)
+    auto time_seq = [&](float* ms_out) -> int {
         float sum = 0;
         for (int r = 0; r <= reps; r++) {
             CU(cudaEventRecord(e0, s), "cudaEventRecord");
-            rc = enqueue(b, n, s, b->d_frames, b->d_bch, b->d_demap, true);
-            if (rc)
-                break;
+            const int rc2 = enqueue(b, n, s, b->d_frames, b->d_bch, b->d_demap, true);
+            if (rc2)
+                return rc2;
             CU(cudaEventRecord(e1, s), "cudaEventRecord");
             CU(cudaEventSynchronize(e1), "cudaEventSynchronize");
             float ms = 0;
+            CU(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+            if (r > 0)
+                sum += ms;
+        }
+        *ms_out = sum / reps;
+        return CUSAT_OK;
+    };
+    std::vector<int> saved_grid(nc);
+    for (int k = 0; k < nc; k++)
+        saved_grid[k] = b->classes[k].grid;
+    // 1. each class's decoder alone on its full grid (its LLRs are in place
+    // after one full sequence): the measured cost that orders the classes
+    std::vector<float> solo(nc, 0.0f);
+    float ms0 = 0;
+    rc = time_seq(&ms0);
+    for (int k = 0; k < nc && rc == CUSAT_OK; k++) {
+        KernelClass& c = b->classes[k];
+        const int cnt = b->class_count[k];
+        if (!cnt)
+            continue;
+        cusat::DecodeArgs a = c.proto;
+        a.frames = b->d_frames + b->class_off[k];
+        a.n_frames = cnt;
+        const int grid = std::min(cnt, c.grid_max);
+        float sum = 0;
+        for (int r = 0; r <= reps; r++) {
+            cudaEventRecord(e0, s);
+            const int lr = cusat::launch_decoder(c.fn, a, grid, c.threads, s);
+            if (lr) {
+                rc = cuda_fail((cudaError_t)lr, "decoder launch");
+                break;
+            }
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             if (r > 0)
-                sum += ms;  // first run warms the caches and the instruction cache
+                sum += ms;
         }
-        if (rc)
-            break;
-        if (sum / reps < best) {
-            best = sum / reps;
-            best_i = ci;
+        solo[k] = sum / reps;
+    }
+    // 2. candidates: class order x grid rule.  Rules 0-3 make each persistent
+    // CTA decode f = 1, 2, 3, 4 frames of its class (grid = count / f, at
+    // most the resident slots); rule 4 shares the SMs in proportion to the
+    // classes' measured cost
+    std::vector<int> by_cost(nc), by_cost_rev;
+    for (int k = 0; k < nc; k++)
+        by_cost[k] = k;
+    std::sort(by_cost.begin(), by_cost.end(), [&](int x, int y) { return solo[x] > solo[y]; });
+    by_cost_rev.assign(by_cost.rbegin(), by_cost.rend());
+    double total = 0;
+    for (float v : solo)
+        total += v;
+    auto frames_per_cta = [&](int k, int f) {
+        const int cnt = b->class_count[k];
+        return std::max(1, std::min(b->classes[k].grid_max, (cnt + f - 1) / f));
+    };
+    auto set_rule = [&](int rule) {
+        for (int k = 0; k < nc; k++) {
+            KernelClass& c = b->classes[k];
+            if (rule <= 3) {
+                c.grid = frames_per_cta(k, rule + 1);
+            } else {
+                const double share = total > 0 ? solo[k] / total : 1.0;
+                c.grid = std::max(1, (int)(share * c.grid_max + 0.5));
+            }
         }
+    };
+    float best = 1e30f;
+    std::vector<int> best_order = by_cost, best_grid(nc, 0);
+    const std::vector<int>* orders[] = {&by_cost, &by_cost_rev};
+    for (int oi = 0; oi < 2 && rc == CUSAT_OK; oi++) {
+        for (int rule = 0; rule < 5 && rc == CUSAT_OK; rule++) {
+            b->order = *orders[oi];
+            set_rule(rule);
+            float ms = 0;
+            if ((rc = time_seq(&ms)) != CUSAT_OK)
+                break;
+            if (ms < best) {
+                best = ms;
+                best_order = b->order;
+                for (int k = 0; k < nc; k++)
+                    best_grid[k] = b->classes[k].grid;
+            }
+        }
+    }
+    // 3. per class, costliest first: frames per CTA in {1, 2, 3, 4, 6, 8}
+    // with the others fixed, kept when it gains at least 0.5 %
+    b->order = best_order;
+    for (int k = 0; k < nc; k++)
+        b->classes[k].grid = best_grid[k];
+    for (int oi = 0; oi < nc && rc == CUSAT_OK; oi++) {
+        const int k = by_cost[oi];
+        if (!b->class_count[k])
+            continue;
+        const int keep = b->classes[k].grid;
+        int best_g = keep;
+        for (int f : {1, 2, 3, 4, 6, 8}) {
+            const int g = frames_per_cta(k, f);
+            if (g == keep)
+                continue;
+            b->classes[k].grid = g;
+            float ms = 0;
+            if ((rc = time_seq(&ms)) != CUSAT_OK)
+                break;
+            if (ms < best * 0.995f) {
+                best = ms;
+                best_g = g;
+            }
+        }
+        b->classes[k].grid = best_g;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rc)
+    if (rc) {
+        for (int k = 0; k < nc; k++)
+            b->classes[k].grid = saved_grid[k];
         return rc;
-    b->order = *cands[best_i].order;
+    }
     for (int k = 0; k < nc; k++)
-        b->classes[k].grid_frac =
-            cands[best_i].rule == 0 ? 1.0f : (float)std::max(0.05, total > 0 ? work[k] / total : 1.0);
+        b->classes[k].tuned_ms = solo[k];
     if (best_ms)
         *best_ms = best;
     return CUSAT_OK;
+}
+
+int cusat_batch_tuned(const cusat_batch* b, int32_t* out, float* solo_ms, int max_classes)
+{
+    if (!b || !out || max_classes < 0)
+        return fail(CUSAT_ERR_ARG, "null argument");
+    const int nc = (int)b->classes.size();
+    for (int k = 0; k < nc && k < max_classes; k++) {
+        const KernelClass& c = b->classes[k];
+        int pos = -1;
+        for (int o = 0; o < (int)b->order.size(); o++)
+            if (b->order[o] == k)
+                pos = o;
+        out[5 * k + 0] = c.cmax;
+        out[5 * k + 1] = c.lanes;
+        const int cnt = k < (int)b->class_count.size() ? b->class_count[k] : 0;
+        const int grid = std::min(c.grid > 0 ? c.grid : c.grid_max, c.grid_max);
+        out[5 * k + 2] = cnt;
+        out[5 * k + 3] = cnt > 0 ? std::min(grid, cnt) : grid;  // what a launch of these frames uses
+        out[5 * k + 4] = pos;
+        if (solo_ms)
+            solo_ms[k] = c.tuned_ms;
+    }
+    return nc;
 }
 
 }  // extern "C"

@@ -243,10 +243,21 @@ int cusat_batch_set_max_ctas(cusat_batch* b, int max_ctas);
  * launch (or replay) at a time per batch object: they share its LLR and
  * message scratch. */
 int cusat_batch_launch(cusat_batch* b, const cusat_frame* frames, int n, void* stream);
-/* Times reps launches of each candidate (class order x grid split) on this
- * frame list and keeps the fastest for later launches and captures. */
+/* Tunes the launch sequence on this frame list (reps timed launches per
+ * candidate) and keeps the fastest for later launches and captures: times
+ * each kernel class's decoder alone; tries class orders (costliest first,
+ * or last) x grid rules (each persistent CTA decoding f = 1, 2, 3 or 4
+ * frames of its class, or CTAs in proportion to the classes' measured
+ * cost); then refines each class's frames per CTA over {1, 2, 3, 4, 6, 8}.
+ * best_ms: the chosen sequence's time. */
 int cusat_batch_tune(cusat_batch* b, const cusat_frame* frames, int n, int reps, void* stream,
                      float* best_ms);
+/* The tuned configuration, per kernel class k < max_classes:
+ * out[5k..5k+4] = circulant slots per layer, lanes, frames of the last
+ * staged list, persistent CTAs, position in the launch order; solo_ms[k]
+ * (may be NULL) = the class's decoder alone at the last tuning.  Returns
+ * the number of classes. */
+int cusat_batch_tuned(const cusat_batch* b, int32_t* out, float* solo_ms, int max_classes);
 /* Captures the launch sequence for this frame list into a CUDA graph
  * (stream must not be the legacy default stream); cusat_batch_replay
  * relaunches it: same frames, same buffers, whatever they hold now. */

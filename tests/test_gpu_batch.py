@@ -167,6 +167,13 @@ def test_graph_replay_and_tuner(mixed):
     assert best > 0
     torch.cuda.synchronize()
     _check(bufs, ref)
+    # the tuned configuration: every class with frames has a grid of 1 ..
+    # frames CTAs, a launch position, and a measured solo time
+    tuned = b.tuned()
+    assert len(tuned) == b.info()[1]
+    used = [c for c in tuned if c["frames"] > 0]
+    assert used and all(1 <= c["ctas"] <= c["frames"] and c["solo_ms"] > 0 for c in used)
+    assert sorted(c["order"] for c in tuned) == list(range(len(tuned)))
     bufs, frames = _buffers(per, order, torch)
     b.capture(frames, s)
     # a launch with other frames between capture and replay leaves the graph intact
