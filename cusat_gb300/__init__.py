@@ -32,7 +32,7 @@ from .enums import *  # noqa: F401,F403
 from .enums import FECFRAME_NORMAL, FECFRAME_SHORT, FECFRAME_MEDIUM  # noqa: F401
 
 __all__ = ["ldpc_decode_cuda", "ldpc_decode", "demapper_cuda", "bch_check_cuda", "rx_fec", "batch", "server",
-           "generator", "bb_extractor", "gpu_decode_budget", "rx_fec_chain", "rx_fec_pool", "dd_snr",
+           "generator", "bb_extractor", "pl_extractor", "pl_layout", "pl_rotation_index", "gpu_decode_budget", "rx_fec_chain", "rx_fec_pool", "dd_snr",
            "code_info", "modcod_info", "encode_frames", "map_frames", "capped_llr_gain",
            "CusatError", "library_path"]
 
@@ -545,6 +545,59 @@ class bb_extractor:
         _capi.check(_capi.lib().cusat_bb_extract(self._h, _addr(hard_dev), hard_stride, _addr(trials_dev),
                                                  _addr(bch_valid_dev), batch, _addr(out_dev), max_out,
                                                  _addr(lengths_dev), _addr(offsets_dev), _stream(stream)))
+
+
+_PL_KEYS = ["slots", "pilots", "pilot_blocks", "data_symbols", "payload_symbols", "modcod", "framesize",
+            "bits_per_symbol", "dummy", "deliverable", "reserved"]
+
+
+def pl_layout(pls_code):
+    """PLFRAME layout of an 8-bit PLS code (reference pl_layout_from_code)."""
+    out = np.zeros(11, np.int32)
+    _capi.check(_capi.lib().cusat_pl_layout(pls_code, out.ctypes.data))
+    return dict(zip(_PL_KEYS, (int(v) for v in out)))
+
+
+def pl_rotation_index(gold, n):
+    """Scrambling rotation index R_n(i), i < n (descrambling factor e^{-j R pi/2})."""
+    r = np.zeros(n, np.uint8)
+    _capi.check(_capi.lib().cusat_pl_rotation_index(gold, r.ctypes.data, n))
+    return r
+
+
+class pl_extractor:
+    """PL receiver tail for located PLFRAMEs (reference
+    pl_receiver::process_payload's data step): descramble, drop the pilot
+    blocks, counter-rotate each slot -> XFECFRAME data symbols (device)."""
+
+    def __init__(self, gold_codes, max_frames=256):
+        g = np.ascontiguousarray(np.asarray(gold_codes, np.int32).reshape(-1))
+        h = ctypes.c_void_p()
+        _capi.check(_capi.lib().cusat_pl_extractor_create(g.ctypes.data, g.size, max_frames, ctypes.byref(h)))
+        self._h = h
+        self.max_frames = max_frames
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().cusat_pl_extractor_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    @staticmethod
+    def frames(payload, data, pls_code, gold, slot_rot=None):
+        """Array of cusat_pl_frame from per-frame lists (addresses or tensors)."""
+        n = len(payload)
+        arr = (_capi.PlFrame * n)()
+        for f in range(n):
+            arr[f] = _capi.PlFrame(_addr(payload[f]), _addr(data[f]),
+                                   None if slot_rot is None or slot_rot[f] is None else _addr(slot_rot[f]),
+                                   int(pls_code[f]), int(gold[f]))
+        return arr
+
+    def extract(self, frames, stream=None):
+        self._frames = frames
+        _capi.check(_capi.lib().cusat_pl_extract(self._h, ctypes.addressof(frames), len(frames), _stream(stream)))
 
 
 def _symbols(symbols):

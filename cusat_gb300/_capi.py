@@ -69,6 +69,12 @@ _SIGS = {
     "cusat_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "cusat_bb_extractor_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_bb_extractor_destroy": (None, [ctypes.c_void_p]),
+    "cusat_pl_layout": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p]),
+    "cusat_pl_rotation_index": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
+    "cusat_pl_extractor_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_void_p)]),
+    "cusat_pl_extractor_destroy": (None, [ctypes.c_void_p]),
+    "cusat_pl_extract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "cusat_bb_extract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -161,6 +167,12 @@ _SIGS = {
     "cusat_modcod_capped_llr_gain": (ctypes.c_float, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                       ctypes.c_float]),
 }
+
+
+class PlFrame(ctypes.Structure):
+    """cusat_pl_frame of include/cusat_fec.h."""
+    _fields_ = [("payload", ctypes.c_void_p), ("data", ctypes.c_void_p), ("slot_rot", ctypes.c_void_p),
+                ("pls_code", ctypes.c_int32), ("gold", ctypes.c_int32)]
 
 
 class Frame(ctypes.Structure):

@@ -376,6 +376,49 @@ int cusat_ldpc_decode_noalloc(int framesize, int rate, int max_trials, const int
                               uint8_t* hard_out, int32_t* trials_out, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* PL receiver tail: located PLFRAMEs -> XFECFRAMEs                         */
+/* ---------------------------------------------------------------------- */
+
+typedef struct cusat_pl_extractor cusat_pl_extractor;
+
+/* One located PLFRAME of a cusat_pl_extract call. */
+typedef struct cusat_pl_frame {
+    const float* payload;   /* device: the symbols after the 90-symbol PLHEADER (re, im), 8-byte aligned */
+    float* data;            /* device: 90 S data symbols out (re, im), 8-byte aligned */
+    const float* slot_rot;  /* device: per slot {rot re, rot im, step re, step im}, 16-byte aligned; NULL = 1 */
+    int32_t pls_code;       /* 8-bit PLS code of the PLHEADER: sets the slots S and the pilot blocks */
+    int32_t gold;           /* PL scrambling (Gold) code n, one of the extractor's */
+} cusat_pl_frame;
+
+/* Replaces pl_layout_from_code (lib/cusat_dsp/framing/plframe.h:66-73,
+ * plframe.cc:221): out[0..10] = slots S, pilots, pilot blocks, data symbols
+ * (90 S), payload symbols (data + 36 per pilot block), MODCOD index, frame
+ * size, bits per symbol, dummy, deliverable (carries an XFECFRAME of a
+ * supported MODCOD and frame size), reserved. */
+int cusat_pl_layout(int pls_code, int32_t* out);
+
+/* The scrambling rotation index R_n(i) (0..3, descrambling factor
+ * e^{-j R pi/2}) of Gold code n for i < len: the sequence the reference's
+ * pl_descrambling_sequence (lib/cusat_dsp/framing/pl_scrambler.h:17-18,
+ * pl_scrambler.cc:47-71) turns into complex factors.  Host only. */
+int cusat_pl_rotation_index(int gold, uint8_t* r, int len);
+
+/* Replaces the data step of pl_receiver::process_payload
+ * (lib/cusat_dsp/plrx/pl_receiver.cc:1694-1741, rotate_slot :1217-1282) for
+ * a batch of frames the host-side synchroniser has located: each frame's
+ * payload is descrambled, its pilot blocks (36 symbols after every 16 slots
+ * when the PLS code signals pilots) are dropped, and slot s is
+ * counter-rotated by slot_rot[s] (rot * step^i for its symbol i, the
+ * reference's arithmetic, non-finite results set to 0) into data.  The
+ * extractor holds the descrambling tables of the given Gold codes.
+ * Asynchronous on `stream`; waits for the previous call's descriptor copy.
+ * Errors: CUSAT_ERR_UNSUPPORTED for a PLS code without a decodable
+ * XFECFRAME (dummy, reserved, unsupported MODCOD or frame size). */
+int cusat_pl_extractor_create(const int32_t* gold_codes, int n_codes, int max_frames, cusat_pl_extractor** out);
+void cusat_pl_extractor_destroy(cusat_pl_extractor* x);
+int cusat_pl_extract(cusat_pl_extractor* x, const cusat_pl_frame* frames, int n, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Post-FEC baseband stage                                                 */
 /* ---------------------------------------------------------------------- */
 

@@ -26,6 +26,9 @@ REF_SOURCES = [
     "lib/cusat_dsp/bbframe_parser.cc",
     "lib/cusat_dsp/bb_header.cc",
     "lib/cusat_dsp/modulation/dd_snr.cc",
+    "lib/cusat_dsp/framing/plframe.cc",
+    "lib/cusat_dsp/framing/pl_scrambler.cc",
+    "lib/cusat_dsp/framing/plheader.cc",
 ]
 
 
@@ -64,12 +67,14 @@ def build_ref(verbose=False):
     out = os.path.join(out_dir, "libcusat_ref_host.so")
     srcs = [os.path.join(REF, s) for s in REF_SOURCES]
     shim = os.path.join(HERE, "ref_shim.cc")
-    if _newer(out, srcs + [shim]):
+    # compiles plrx/pl_receiver.cc in place (its slot de-rotation is file-local)
+    plrx_shim = os.path.join(HERE, "ref_plrx_shim.cc")
+    if _newer(out, srcs + [shim, plrx_shim, os.path.join(REF, "lib", "cusat_dsp", "plrx", "pl_receiver.cc")]):
         return out
     inc = ["-I" + os.path.join(REF, "lib", "cusat_dsp"),
            "-I" + os.path.join(REF, "lib", "cusat_dsp", "include")]
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", *inc,
-           "-o", out + ".tmp", shim, *srcs]
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-w", *inc,
+           "-o", out + ".tmp", shim, plrx_shim, *srcs]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)

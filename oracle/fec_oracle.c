@@ -981,3 +981,95 @@ float orc_dd_snr(const float* sym, int n_sym, const float* pts, int n_points, in
         return 0.0f;
     return err * 1e6f <= sig ? 1e6f : sig / err;
 }
+
+/* ------------------------------------------------------------------------ */
+/* PL receiver tail: descrambling and pilot removal                          */
+/* ------------------------------------------------------------------------ */
+
+/* Rotation index R_n(i) of the PLFRAME scrambler (EN 302 307-1 clause
+ * 5.5.4; reference framing/pl_scrambler.cc:47-71): the m-sequences
+ * x(i + 18) = x(i + 7) + x(i), x(0) = 1, x(1..17) = 0, and
+ * y(i + 18) = y(i + 10) + y(i + 7) + y(i + 5) + y(i), y(0..17) = 1 (mod 2),
+ * period P = 2^18 - 1, are written out in full; z_n(i) = x(i + n) + y(i) and
+ * R_n(i) = 2 z_n(i + 2^17) + z_n(i), indices mod P.  The descrambling
+ * factor is e^{-j R pi/2}.  Returns -1 for n outside 0 .. 2^18 - 3. */
+#define PL_PERIOD 262143
+int orc_pl_rotation(int gold, uint8_t* r, int len)
+{
+    if (gold < 0 || gold >= PL_PERIOD - 1 || len < 0)
+        return -1;
+    uint8_t* x = (uint8_t*)malloc(PL_PERIOD + 18);
+    uint8_t* y = (uint8_t*)malloc(PL_PERIOD + 18);
+    memset(x, 0, 18);
+    x[0] = 1;
+    memset(y, 1, 18);
+    for (int i = 0; i + 18 < PL_PERIOD + 18; i++) {
+        x[i + 18] = x[i + 7] ^ x[i];
+        y[i + 18] = y[i + 10] ^ y[i + 7] ^ y[i + 5] ^ y[i];
+    }
+    for (int i = 0; i < len; i++) {
+        const int i0 = i % PL_PERIOD, i1 = (i + 131072) % PL_PERIOD;
+        const int z0 = x[(i0 + gold) % PL_PERIOD] ^ y[i0];
+        const int z1 = x[(i1 + gold) % PL_PERIOD] ^ y[i1];
+        r[i] = (uint8_t)(2 * z1 + z0);
+    }
+    free(x);
+    free(y);
+    return 0;
+}
+
+/* The data symbols of one located PLFRAME (reference plrx/pl_receiver.cc
+ * :1694-1741 with rotate_slot :1217-1282): payload = the symbols after the
+ * 90-symbol PLHEADER; slot s (90 symbols) starts at s * 90 + min(s / 16,
+ * pilot blocks) * 36 (a 36-symbol pilot block after every 16 slots,
+ * (slots - 1) / 16 blocks when pilots are on); each symbol is descrambled
+ * (times e^{-j R pi/2}) and counter-rotated: symbol i of the slot is
+ * multiplied by rot * step^i, with the powers built as four interleaved
+ * chains (chain c = i mod 4 starts at rot * step^c and advances by step^4),
+ * every product in the reference's order, no contraction; non-finite
+ * results become 0.  slot_rot: per slot {rot re, rot im, step re, step im},
+ * or NULL for rot = step = 1.  out: 90 * slots (re, im) pairs. */
+int orc_pl_extract(const float* payload, int slots, int pilots, const uint8_t* r, const float* slot_rot, float* out)
+{
+    static const float ROT_RE[4] = {1.0f, 0.0f, -1.0f, 0.0f};
+    static const float ROT_IM[4] = {0.0f, -1.0f, 0.0f, 1.0f};
+    if (slots <= 0 || !payload || !r || !out)
+        return -1;
+    const int n_pb = pilots ? (slots - 1) / 16 : 0;
+    for (int s = 0; s < slots; s++) {
+        const int off = s * 90 + (s / 16 < n_pb ? s / 16 : n_pb) * 36;
+        const float rr = slot_rot ? slot_rot[4 * s] : 1.0f, ri = slot_rot ? slot_rot[4 * s + 1] : 0.0f;
+        const float sr = slot_rot ? slot_rot[4 * s + 2] : 1.0f, si = slot_rot ? slot_rot[4 * s + 3] : 0.0f;
+        float cr[4], ci[4];
+        cr[0] = rr;
+        ci[0] = ri;
+        for (int c = 1; c < 4; c++) {
+            cr[c] = cr[c - 1] * sr - ci[c - 1] * si;
+            ci[c] = cr[c - 1] * si + ci[c - 1] * sr;
+        }
+        float pr = sr, pi = si;
+        for (int c = 1; c < 4; c++) {
+            const float t = pr * sr - pi * si;
+            pi = pr * si + pi * sr;
+            pr = t;
+        }
+        float* o = out + 2 * (size_t)s * 90;
+        for (int i = 0; i < 90; i++) {
+            const int c = i & 3, k = off + i;
+            const float ar = payload[2 * k], ai = payload[2 * k + 1];
+            const float br = ROT_RE[r[k] & 3], bi = ROT_IM[r[k] & 3];
+            const float xr = ar * br - ai * bi, xi = ar * bi + ai * br;
+            float vr = xr * cr[c] - xi * ci[c], vi = xr * ci[c] + xi * cr[c];
+            if (i < 88) {  /* the chains advance once per group of four */
+                const float nr = cr[c] * pr - ci[c] * pi;
+                ci[c] = cr[c] * pi + ci[c] * pr;
+                cr[c] = nr;
+            }
+            if (!isfinite(vr) || !isfinite(vi))
+                vr = vi = 0.0f;
+            o[2 * i] = vr;
+            o[2 * i + 1] = vi;
+        }
+    }
+    return 0;
+}

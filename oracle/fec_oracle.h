@@ -112,6 +112,15 @@ int orc_bb_build(const uint8_t* data, int len, int kbch, int matype_ts_gs, uint8
  * every stride-th symbol.  Reference modulation/dd_snr.cc:12-47. */
 float orc_dd_snr(const float* sym, int n_sym, const float* pts, int n_points, int stride, int qpsk);
 
+/* PL receiver tail (EN 302 307-1 clause 5.5.4; reference
+ * framing/pl_scrambler.cc, plrx/pl_receiver.cc:1694-1741): the
+ * descrambling rotation index R_n(i) (factor e^{-j R pi/2}) of gold code n
+ * for i < len, and the data symbols of one located PLFRAME's payload
+ * (descramble, drop the pilot blocks, counter-rotate each slot by
+ * rot * step^i; slot_rot may be NULL). */
+int orc_pl_rotation(int gold, uint8_t* r, int len);
+int orc_pl_extract(const float* payload, int slots, int pilots, const uint8_t* r, const float* slot_rot, float* out);
+
 /* Unrolled learned min-sum (training model; nms_model.inc): loss and its
  * gradient with respect to theta[T][32][2] = {beta, alpha} per iteration and
  * check degree, summed over B frames of int16 LLRs and packed codewords

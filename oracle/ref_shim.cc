@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
+#include <vector>
 
 #include "fec/bch_code.h"
 #include "fec/code_params.h"
@@ -16,6 +17,8 @@
 #include "bb_header.h"
 #include "bb_scrambler.h"
 #include "bbframe_parser.h"
+#include "framing/pl_scrambler.h"
+#include "framing/plframe.h"
 
 using namespace cusat_dsp;
 
@@ -145,3 +148,36 @@ int ref_build_bbframe(int fs, int rate, const uint8_t* data, int len, uint8_t* o
 }
 
 }
+
+extern "C" {
+
+// pl_layout_from_code (framing/plframe.cc:221): out = slots, pilots, pilot
+// blocks, data symbols, payload symbols, MODCOD index, frame size, bits per
+// symbol, dummy, deliverable, reserved
+int ref_pl_layout(int code, int32_t* out)
+{
+    const pl_layout l = pl_layout_from_code((uint8_t)code);
+    out[0] = l.slots; out[1] = l.pilots; out[2] = l.pilot_block_count(); out[3] = l.data_symbols();
+    out[4] = l.payload_symbols(); out[5] = l.modcod; out[6] = (int)l.fec_size; out[7] = l.bits_per_symbol;
+    out[8] = l.dummy; out[9] = l.deliverable(); out[10] = l.reserved;
+    return 0;
+}
+
+// pl_descrambling_sequence (framing/pl_scrambler.cc:47-71): the factors as
+// (re, im) float pairs
+int ref_pl_descrambling(int gold, float* seq, int len)
+{
+    try {
+        std::vector<complexf> v(len);
+        pl_descrambling_sequence(gold, v.data(), len);
+        for (int i = 0; i < len; i++) {
+            seq[2 * i] = v[i].real();
+            seq[2 * i + 1] = v[i].imag();
+        }
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -8,7 +8,8 @@ on machines without the reference tree.
 Contents: FEC dimensions and BCH generators of every supported (frame size,
 rate); BCH codewords of seeded messages; interleaver column offsets and
 constellation points (as float32 bit patterns) of every MODCOD; the BB
-scrambler PRBS; the demapper's loudest-bit distance (dmax, which sets the
+scrambler PRBS; PLFRAME layouts of all 256 PLS codes and PL scrambling
+sequences; the demapper's loudest-bit distance (dmax, which sets the
 LLR gain cap) of every MODCOD's reference points; GSE BBFRAMEs built by the reference and its data-field
 extraction of them; decision-directed SNR estimates of seeded symbols."""
 import ctypes
@@ -44,6 +45,22 @@ def dd_symbols(seed, n=2000):
         s = np.random.default_rng(7).integers(0, 2, 2 * n) * 2 - 1
         return (s * a).astype(np.float32)
     return np.random.default_rng(seed).uniform(-1.3, 1.3, 2 * n).astype(np.float32)
+
+
+PL_GOLDS = [0, 1, 5, 77777, 262141]
+PL_LEN = 33192  # the longest PLFRAME payload (QPSK normal frame with pilots)
+
+
+def pl_index(seq):
+    """Rotation index R (factor e^{-j R pi/2}) from (re, im) factor pairs."""
+    re, im = seq[0::2], seq[1::2]
+    r = np.full(re.size, 255, np.uint8)
+    r[(re == 1) & (im == 0)] = 0
+    r[(re == 0) & (im == -1)] = 1
+    r[(re == -1) & (im == 0)] = 2
+    r[(re == 0) & (im == 1)] = 3
+    assert (r != 255).all()
+    return r
 
 
 def main():
@@ -107,6 +124,20 @@ def main():
         v = ref.ref_dd_snr(mod, rate, fs, p(sym), len(sym) // 2, stride, 1 if mod == 0 else 0)
         doc["dd_snr"].append({"mod": mod, "rate": rate, "fs": fs, "stride": stride, "seed": seed,
                               "value": int(np.float32(v).view(np.uint32))})
+    # PLFRAME layouts of every PLS code and scrambling sequences (rotation
+    # index R per symbol, from the reference's descrambling factors)
+    doc["pl_layouts"] = []
+    for code in range(256):
+        out = np.zeros(11, np.int32)
+        ref.ref_pl_layout(code, p(out))
+        doc["pl_layouts"].append([int(v) for v in out])
+    doc["pl_rotation"] = []
+    for gold in PL_GOLDS:
+        seq = np.zeros(2 * PL_LEN, np.float32)
+        assert ref.ref_pl_descrambling(gold, p(seq), PL_LEN) == 0
+        r = pl_index(seq)
+        doc["pl_rotation"].append({"gold": gold, "len": PL_LEN, "head": "".join(str(int(v)) for v in r[:96]),
+                                   "sha256": hashlib.sha256(r.tobytes()).hexdigest()})
     path = os.path.join(HERE, "reference_host.json")
     with open(path, "w") as f:
         json.dump(doc, f, separators=(",", ":"))

@@ -264,3 +264,44 @@ def dd_snr(sym, pts, stride=1, qpsk=False):
     pts = np.ascontiguousarray(pts, np.float32)
     return float(lib().orc_dd_snr(_p(sym, ctypes.c_float), sym.size // 2, _p(pts, ctypes.c_float),
                                   pts.size // 2, stride, 1 if qpsk else 0))
+
+
+def pl_rotation(gold, n):
+    """The oracle's PL scrambling rotation index R_n(i), i < n."""
+    r = np.zeros(n, np.uint8)
+    assert lib().orc_pl_rotation(gold, _p(r, ctypes.c_uint8), n) == 0
+    return r
+
+
+def pl_extract(payload, slots, pilots, r, slot_rot=None):
+    """The oracle's data symbols of one PLFRAME payload ((re, im) pairs)."""
+    payload = np.ascontiguousarray(payload, np.float32)
+    r = np.ascontiguousarray(r, np.uint8)
+    out = np.zeros(2 * 90 * slots, np.float32)
+    rot = None if slot_rot is None else _p(np.ascontiguousarray(slot_rot, np.float32), ctypes.c_float)
+    assert lib().orc_pl_extract(_p(payload, ctypes.c_float), slots, 1 if pilots else 0, _p(r, ctypes.c_uint8), rot,
+                                _p(out, ctypes.c_float)) == 0
+    return out
+
+
+def pl_frame_payload(data, slots, pilots, r):
+    """Test traffic for the PL receiver tail: the transmitted payload of one
+    PLFRAME -- data slots with a pilot block (36 symbols (1 + j)/sqrt 2)
+    after every 16 slots when pilots are on (EN 302 307-1 clause 5.5.3),
+    scrambled by e^{+j R pi/2} (clause 5.5.4)."""
+    data = np.asarray(data, np.float32).reshape(-1, 2)
+    n_pb = (slots - 1) // 16 if pilots else 0
+    a = np.float32(np.sqrt(0.5))
+    rows = []
+    for s in range(slots):
+        rows.append(data[90 * s:90 * (s + 1)])
+        if pilots and s % 16 == 15 and (s + 1) // 16 <= n_pb:
+            rows.append(np.tile(np.array([[a, a]], np.float32), (36, 1)))
+    pay = np.concatenate(rows)
+    rr = r[:len(pay)] & 3
+    re, im = pay[:, 0].copy(), pay[:, 1].copy()
+    out = np.empty_like(pay)
+    # e^{+j R pi/2}: 1, j, -1, -j
+    out[:, 0] = np.select([rr == 0, rr == 1, rr == 2, rr == 3], [re, -im, -re, im])
+    out[:, 1] = np.select([rr == 0, rr == 1, rr == 2, rr == 3], [im, re, -im, -re])
+    return out.reshape(-1)
