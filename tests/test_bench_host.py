@@ -50,3 +50,17 @@ def test_reference_arm_loads_only_the_oracle():
     nb = bench.n_bufs_for(wl, bench.OracleGen())
     sym_bytes = wl["frames"] * bench.OracleGen().modcod_info(wl["mod"], wl["rate"], wl["fs"])["xfecframe_len"] * 8
     assert line["config"] == bench.single_config(wl, nb, sym_bytes)
+
+
+def test_pl_workload_traffic(built_lib):
+    """bench.py's PLFRAME builder (pilots + scrambling) equals the oracle's,
+    and the oracle's receiver tail recovers the XFECFRAMEs exactly."""
+    import bench
+    import cusat_gb300 as cs
+    import oracle_lib as O
+    ci, msg, bufs, n0, gain = bench.make_traffic(dict(bench.WORKLOAD, frames=3), 1)
+    pay, lay = bench.pl_frames(cs, bufs[0], (12 << 2) | 1, 0)
+    r = O.pl_rotation(0, lay["payload_symbols"])
+    for f in range(3):
+        assert np.array_equal(pay[f], O.pl_frame_payload(bufs[0][f], lay["slots"], 1, r))
+        assert np.array_equal(O.pl_extract(pay[f], lay["slots"], 1, r), bufs[0][f])
