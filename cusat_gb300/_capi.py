@@ -70,6 +70,7 @@ _SIGS = {
     "cusat_bb_extractor_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_bb_extractor_destroy": (None, [ctypes.c_void_p]),
     "cusat_pl_layout": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p]),
+    "cusat_ldpc_encode": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_pl_rotation_index": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_int]),
     "cusat_pl_extractor_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                  ctypes.POINTER(ctypes.c_void_p)]),

@@ -630,6 +630,18 @@ int cusat_gen_encode(int framesize, int rate, const uint8_t* msg, uint8_t* cw, i
     return CUSAT_OK;
 }
 
+int cusat_ldpc_encode(int framesize, int rate, const uint8_t* info, uint8_t* cw, int batch)
+{
+    if (!info || !cw || batch < 0)
+        return fail(CUSAT_ERR_ARG, "invalid arguments");
+    std::string err;
+    const cusat::CodePlan* p = cusat::get_code_plan(framesize, rate, &err);
+    if (!p)
+        return fail(CUSAT_ERR_UNSUPPORTED, err);
+    cusat::ldpc_encode_frames(*p, info, cw, batch);
+    return CUSAT_OK;
+}
+
 int cusat_gen_map(int modulation, int rate, int framesize, const uint8_t* cw, int batch, float* sym)
 {
     if (!cw || !sym || batch < 0)

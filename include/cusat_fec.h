@@ -594,6 +594,12 @@ int cusat_generate(cusat_generator* g, const uint8_t* msg_dev, int batch, uint8_
  * Reference get_fec_params (lib/cusat_dsp/fec/code_params.cc:102-108) and
  * create_ldpc_table (lib/cusat_dsp/ldpc_table_factory.cc:97-102). */
 int cusat_code_info(int framesize, int rate, int32_t* out);
+/* Replaces ldpc_encode::encode (lib/cusat_dsp/ldpc_encode.h:31, the
+ * systematic IRA encoder of EN 302 307 Annex C): batch codewords, k_ldpc/8
+ * info bytes in (the BCH codeword), n_ldpc/8 bytes out (info then parity,
+ * MSB first).  Host code; test traffic and the reference's encode callers. */
+int cusat_ldpc_encode(int framesize, int rate, const uint8_t* info, uint8_t* cw, int batch);
+
 /* BCH + LDPC encode: msg k_bch/8 bytes -> codeword n_ldpc/8 bytes per frame
  * (reference bch_encode fec/bch_code.cc:124-144, IRA encoder
  * ldpc_encode.cc:6-13). */

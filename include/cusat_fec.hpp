@@ -280,6 +280,73 @@ class ldpc_decode
     int max_batch_ = 0;
 };
 
+// Reference lib/cusat_dsp/ldpc_encode.h:18-84 (the systematic IRA encoder,
+// for the reference's transmit-side and test callers; not on the receive
+// path).  The codewords are computed on the host (cusat_ldpc_encode); the
+// *_to_device variants copy them on the caller's stream, the D2D variant
+// reads the info bits back first.
+class ldpc_encode
+{
+  public:
+    ldpc_encode(fecframe_size_t framesize, code_rate_t rate) : fs_((int)framesize), rate_((int)rate)
+    {
+        int32_t info[12];
+        const int rc = cusat_code_info(fs_, rate_, info);
+        if (rc)
+            cusat_shim::die(rc, "ldpc_encode");
+        n_ = (unsigned)info[0];
+        k_ = (unsigned)info[1];
+    }
+    ldpc_encode(const ldpc_encode&) = delete;
+    ldpc_encode& operator=(const ldpc_encode&) = delete;
+
+    void encode(const uint8_t* info_in, uint8_t* codeword_out)
+    {
+        const int rc = cusat_ldpc_encode(fs_, rate_, info_in, codeword_out, 1);
+        if (rc)
+            cusat_shim::die(rc, "ldpc_encode::encode");
+    }
+    void encode_to_device(const uint8_t* info_packed_host, uint8_t* fecframe_device, void* cuda_stream)
+    {
+        encode_batch_to_device(info_packed_host, fecframe_device, 1, cuda_stream);
+    }
+    void encode_batch_to_device(const uint8_t* info_packed_host, uint8_t* fecframes_device, int batch_size,
+                                void* cuda_stream)
+    {
+        if (batch_size <= 0)
+            return;
+        buf_.resize((size_t)batch_size * n_bytes());
+        const int rc = cusat_ldpc_encode(fs_, rate_, info_packed_host, buf_.data(), batch_size);
+        if (rc)
+            cusat_shim::die(rc, "ldpc_encode::encode_batch_to_device");
+        // a pageable source is staged before the call returns
+        if (cudaMemcpyAsync(fecframes_device, buf_.data(), buf_.size(), cudaMemcpyHostToDevice,
+                            (cudaStream_t)cuda_stream) != cudaSuccess)
+            cusat_shim::die(CUSAT_ERR_CUDA, "ldpc_encode copy");
+    }
+    void encode_batch_d2d(const uint8_t* info_packed_device, uint8_t* fecframes_device, int batch_size,
+                          void* cuda_stream)
+    {
+        if (batch_size <= 0)
+            return;
+        std::vector<uint8_t> info((size_t)batch_size * k_bytes());
+        if (cudaMemcpyAsync(info.data(), info_packed_device, info.size(), cudaMemcpyDeviceToHost,
+                            (cudaStream_t)cuda_stream) != cudaSuccess ||
+            cudaStreamSynchronize((cudaStream_t)cuda_stream) != cudaSuccess)
+            cusat_shim::die(CUSAT_ERR_CUDA, "ldpc_encode read-back");
+        encode_batch_to_device(info.data(), fecframes_device, batch_size, cuda_stream);
+    }
+    unsigned int n_bits() const { return n_; }
+    unsigned int k_bits() const { return k_; }
+    unsigned int n_bytes() const { return n_ / 8; }
+    unsigned int k_bytes() const { return k_ / 8; }
+
+  private:
+    int fs_, rate_;
+    unsigned n_ = 0, k_ = 0;
+    std::vector<uint8_t> buf_;
+};
+
 
 // Reference lib/cusat_dsp/rx_fec_chain.h:52-59.  The cap lives in the
 // library; chains share it through set_decode_budget.
