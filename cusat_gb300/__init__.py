@@ -182,6 +182,13 @@ class ldpc_decode_cuda:
         several frames of a batch in turn."""
         _capi.check(_capi.lib().cusat_ldpc_decoder_set_max_ctas(self._h, max_ctas))
 
+    def frames_per_cta(self):
+        """2 when this decoder runs frame pairs (short frames, no learned
+        weights), else 1."""
+        n = _capi.lib().cusat_ldpc_decoder_frames_per_cta(self._h)
+        _capi.check(min(n, 0))
+        return n
+
     def results(self, batch_size):
         hard = np.zeros((batch_size, self._kb), np.uint8)
         trials = np.zeros(batch_size, np.int32)

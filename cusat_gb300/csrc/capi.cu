@@ -37,6 +37,14 @@ struct Engine {
     int max_ctas = 0;                 // test hook: cap on the persistent grid (0 = none)
     cudaEvent_t last = nullptr;       // recorded after every launch
     bool launched = false;
+    // Two frames per CTA (codes decoded one layer per step whose frame pair
+    // fits twice per SM: the short frames): pair_fn decodes the frames of
+    // the saturation-free path, then the one-frame kernel the frames it
+    // listed.  nullptr: one-frame kernel only.
+    const void* pair_fn = nullptr;
+    cusat::DecodeArgs pair_layout{};  // its shared-memory carve-up and message stride
+    int pair_grid_max = 0;
+    int* list = nullptr;              // [max_batch] frames left to the one-frame kernel
 
     int set_weights(const int16_t* w, int n_iter)
     {
@@ -89,20 +97,76 @@ struct Engine {
         // no launch runs more CTAs than frames: message scratch for at most
         // max_batch of them
         grid_max = per_sm * sms < batch ? per_sm * sms : batch;
-        const size_t msg_bytes = (size_t)grid_max * p->R * p->msg_row;
+        size_t msg_bytes = (size_t)grid_max * p->R * p->msg_row;
+        if (p->lanes == 1) {
+            const void* pf = cusat::select_pair_kernel(p->cmax);
+            cusat::DecodeArgs pl{};
+            cusat::pair_smem_layout(&pl, cusat::smem_dims_of(proto.code, 1), p->max_stage);
+            int pair_per_sm = 0;
+            if (pf && pl.sm_total <= optin) {
+                CU(allow_full_smem(pf), "cudaFuncSetAttribute");
+                CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pair_per_sm, pf, cusat::kPairThreads, pl.sm_total),
+                   "occupancy");
+            }
+            // a frame pair pays when two of them are resident per SM
+            if (pair_per_sm >= 2) {
+                pair_fn = pf;
+                pair_layout = pl;
+                pair_layout.msg_stride = p->R * cusat::pair_msg_row(p->cmax) / 16;
+                const int pairs = (batch + 1) / 2;
+                pair_grid_max = pair_per_sm * sms < pairs ? pair_per_sm * sms : pairs;
+                const size_t pair_bytes = (size_t)pair_grid_max * pair_layout.msg_stride * 16;
+                if (pair_bytes > msg_bytes)
+                    msg_bytes = pair_bytes;
+                CU(cudaMalloc(&list, (size_t)batch * sizeof(int)), "cudaMalloc(frame list)");
+            }
+        }
         CU(cudaMalloc(&msg, msg_bytes), "cudaMalloc(messages)");
         CU(cudaMalloc(&queue, 256), "cudaMalloc(queue)");
         CU(cudaEventCreateWithFlags(&last, cudaEventDisableTiming), "cudaEventCreate");
-        CU(cudaMemset(queue, 0, 256), "cudaMemset(queue)");  // the kernel rearms it after each launch
+        // frame/exit counters and the list length: the kernels rearm them
+        CU(cudaMemset(queue, 0, 256), "cudaMemset(queue)");
         proto.msg = msg;
         proto.msg_stride = p->R * p->msg_row / 16;
         proto.queue = queue;
         return CUSAT_OK;
     }
 
+    int frames_per_cta() const { return pair_fn && !proto.code.weights ? 2 : 1; }
+
     int launch(cusat::DecodeArgs a, int batch, cudaStream_t stream)
     {
         a.n_frames = batch;
+        if (pair_fn && !a.code.weights) {
+            // frame pairs, then the one-frame kernel over the frames they
+            // listed (usually none: its CTAs exit at once)
+            cusat::DecodeArgs b = a;
+            const cusat::DecodeArgs& l = pair_layout;
+            b.sm_dummy = l.sm_dummy;
+            b.sm_stage = l.sm_stage;
+            b.sm_tab = l.sm_tab;
+            b.sm_cnt = l.sm_cnt;
+            b.sm_sched = l.sm_sched;
+            b.sm_conf = l.sm_conf;
+            b.sm_item_off = l.sm_item_off;
+            b.sm_items = l.sm_items;
+            b.sm_code = l.sm_code;
+            b.sm_misc = l.sm_misc;
+            b.sm_msgbuf = l.sm_msgbuf;
+            b.sm_total = l.sm_total;
+            b.max_stage = l.max_stage;
+            b.msg_stride = l.msg_stride;
+            b.list = list;
+            b.list_count = queue + 4;
+            int pgrid = (batch + 1) / 2 < pair_grid_max ? (batch + 1) / 2 : pair_grid_max;
+            if (max_ctas > 0 && pgrid > max_ctas)
+                pgrid = max_ctas;
+            const int rc = cusat::launch_decoder(pair_fn, b, pgrid, cusat::kPairThreads, stream);
+            if (rc != 0)
+                return cuda_fail((cudaError_t)rc, "decoder launch (frame pairs)");
+            a.list = list;
+            a.list_count = queue + 4;
+        }
         int grid = batch < grid_max ? batch : grid_max;
         if (max_ctas > 0 && grid > max_ctas)
             grid = max_ctas;
@@ -122,6 +186,9 @@ struct Engine {
             cudaFree(msg);
         if (queue)
             cudaFree(queue);
+        if (list)
+            cudaFree(list);
+        list = nullptr;
         weights.release();
         if (last)
             cudaEventDestroy(last);
@@ -224,6 +291,13 @@ int cusat_ldpc_decoder_set_max_ctas(cusat_ldpc_decoder* d, int max_ctas)
         return fail(CUSAT_ERR_ARG, "null decoder or negative CTA cap");
     d->eng.max_ctas = max_ctas;
     return CUSAT_OK;
+}
+
+int cusat_ldpc_decoder_frames_per_cta(const cusat_ldpc_decoder* d)
+{
+    if (!d)
+        return fail(CUSAT_ERR_ARG, "null decoder");
+    return d->eng.frames_per_cta();
 }
 
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* d, int32_t* out)

@@ -35,11 +35,12 @@ constexpr bool stage_rows_in_smem(int cmax, int lanes) { return cmax == 9 && lan
 //       0 when the circulant is the only writer of its group in the step;
 //       otherwise the bit's entry in this circulant's stage row
 //   w = kind: 0 plain, 1 staged, 2 absent (the layer has fewer circulants
-//       than the kernel's slots: reads a region of +32767, writes a junk
+//       than the kernel's slots: reads a region of +32640, writes a junk
 //       region, contributes nothing)
 // x and z of staged and absent slots are relative to the stage/dummy
-// regions and are rebased when the kernel copies the table to shared memory,
-// where each descriptor is packed to a uint2 {x, y | z << 9} (z < 2^22).
+// regions and are rebased when a kernel copies the table to shared memory
+// (y becomes 2 r there; the frame-pair kernel also doubles the APP offsets
+// and places the stage rows in its own sets).
 // When several circulants of one step share an information group, each
 // writes its updated bits to its own int16 stage row, and a group item of
 // the step (uint2: x = byte offset of the group, y = first row | rows << 8)

@@ -50,6 +50,16 @@ int decoder_threads(int lanes);
 // reference (cuda/ldpc_decode_kernel.cu:1237-1241).
 int syndrome_period();
 int launch_decoder(const void* fn, const DecodeArgs& a, int grid, int threads, cudaStream_t stream);
+// The frame-pair kernel (two frames per CTA, single-code launches of codes
+// decoded one layer per step) for cmax, or nullptr; its threads per CTA;
+// its shared-memory carve-up for codes up to d with max_stage stage rows per
+// set (also sets a->max_stage).
+const void* select_pair_kernel(int cmax);
+constexpr int kPairThreads = 384;
+void pair_smem_layout(DecodeArgs* a, const SmemDims& d, int max_stage);
+// Bytes of one check row of messages in the frame-pair kernel (two frames'
+// bytes per edge, whole 16-byte words).
+int pair_msg_row(int cmax);
 
 int launch_demap(const DevDemap& d, const float* sym, int batch, float noise_var, float llr_gain,
                  int16_t* out, cudaStream_t stream);

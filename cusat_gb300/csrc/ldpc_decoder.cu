@@ -3,6 +3,7 @@
 
 #include "kernels.h"
 #include "ldpc_kernel.cuh"
+#include "ldpc_pair.cuh"
 
 namespace cusat {
 
@@ -32,6 +33,23 @@ const void* select_decoder_kernel(int cmax, int lanes)
 }
 
 int decoder_threads(int lanes) { return lanes * lane_threads(lanes); }
+
+static_assert(kPairThreads == lane_threads(1), "the frame-pair kernel runs one lane");
+
+const void* select_pair_kernel(int cmax)
+{
+    switch (cmax) {
+    case 3: return (const void*)ldpc_pair_kernel<3>;
+    case 5: return (const void*)ldpc_pair_kernel<5>;
+    case 9: return (const void*)ldpc_pair_kernel<9>;
+    case 14: return (const void*)ldpc_pair_kernel<14>;
+    case 20: return (const void*)ldpc_pair_kernel<20>;
+    case 28: return (const void*)ldpc_pair_kernel<28>;
+    default: return nullptr;
+    }
+}
+
+int pair_msg_row(int cmax) { return (2 * (cmax + 2) + 15) / 16 * 16; }
 
 int syndrome_period()
 {
@@ -63,6 +81,28 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     const int rw = (d.cmax + 2 + 15) / 16;
     take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * lane_threads(d.lanes) * rw * 16 : 0);
     a->sm_total = off;
+}
+
+void pair_smem_layout(DecodeArgs* a, const SmemDims& d, int max_stage)
+{
+    int off = align16(d.N * 4);  // APP words: frame A's int16 in the low half, B's in the high half
+    auto take = [&](int* field, int bytes) {
+        *field = off;
+        off = align16(off + bytes);
+    };
+    take(&a->sm_dummy, 2 * kM * 4);  // +32640 region, then the junk region
+    take(&a->sm_stage, kStageSets * max_stage * kM * 4);
+    take(&a->sm_tab, d.q * d.cmax * 16);
+    take(&a->sm_cnt, d.q);
+    take(&a->sm_sched, d.n_steps * 4);
+    take(&a->sm_conf, d.n_steps);
+    take(&a->sm_item_off, (d.n_steps + 1) * 2);
+    take(&a->sm_items, d.n_items * 8);
+    take(&a->sm_code, (int)sizeof(DevCode));
+    take(&a->sm_misc, (int)sizeof(PairState));
+    take(&a->sm_msgbuf, 0);
+    a->sm_total = off;
+    a->max_stage = max_stage;
 }
 
 SmemDims smem_dims_of(const DevCode& c, int lanes)

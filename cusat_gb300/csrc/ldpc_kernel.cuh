@@ -69,6 +69,14 @@ struct DecodeArgs {
     uint4* msg;              // [gridDim.x][msg_stride] scratch
     int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
     unsigned int* queue;     // [0] frame counter, [1] CTAs done: zero at launch, zeroed again by the last CTA
+    // Frame lists between the frame-pair kernel and the one-frame kernel
+    // (single code): the pair kernel appends the frames that need the
+    // saturating arithmetic to list; a one-frame launch with list non-null
+    // decodes list[0..*list_count) only, and its last CTA out zeroes
+    // *list_count.  nullptr otherwise.
+    int* list;
+    unsigned int* list_count;
+    int max_stage;           // frame-pair kernel: stage rows per set (the plan's busiest step)
     // shared-memory carve-up (bytes)
     int sm_dummy, sm_stage, sm_tab, sm_cnt, sm_sched, sm_conf, sm_item_off, sm_items, sm_code, sm_misc, sm_msgbuf,
         sm_total;
@@ -763,14 +771,18 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), min_ctas_per_sm(C
         // = 32386) and above 127, so it never changes a message
         dummy[k] = 32640;
     int loaded = -1;
+    // the list is complete when this launch starts (stream order); every CTA
+    // reads its length before its exit count, so before the reset below
+    const int n_frames = a.list ? min((int)*a.list_count, a.n_frames) : a.n_frames;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0)
             s_misc[0] = (int)atomicAdd(a.queue, 1u);
         __syncthreads();
-        const int f = s_misc[0];
-        if (f >= a.n_frames)
+        const int ticket = s_misc[0];
+        if (ticket >= n_frames)
             break;
+        const int f = a.list ? a.list[ticket] : ticket;
         Job job;
         int code_id = 0;
         if (a.frames) {
@@ -805,6 +817,8 @@ __global__ void __launch_bounds__(LANES * lane_threads(LANES), min_ctas_per_sm(C
         if (atomicAdd(a.queue + 1, 1u) == gridDim.x - 1) {
             atomicExch(a.queue, 0u);
             atomicExch(a.queue + 1, 0u);
+            if (a.list)
+                atomicExch(a.list_count, 0u);
         }
     }
 }

@@ -60,6 +60,13 @@ void cusat_ldpc_decoder_destroy(cusat_ldpc_decoder* dec);
  * lanes (2 = paired-layer schedule) */
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* dec, int32_t* out);
 
+/* Frames one CTA of this decoder holds: 2 when it decodes frame pairs (codes
+ * decoded one layer per step whose pair fits twice per SM -- the short
+ * frames -- without learned weights; frames with channel LLRs beyond the
+ * saturation-free range then go to a one-frame launch), else 1.  Results do
+ * not depend on it. */
+int cusat_ldpc_decoder_frames_per_cta(const cusat_ldpc_decoder* dec);
+
 /* Learned min-sum weights (no counterpart in the reference, whose
  * normalised-min-sum hook nms_scale, ldpc_decode_kernel.cu:75-90, is never
  * enabled).  weights[(t * 32 + d) * 2 + {0, 1}] = {beta, alpha} for
