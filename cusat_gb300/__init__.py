@@ -182,10 +182,15 @@ class ldpc_decode_cuda:
         several frames of a batch in turn."""
         _capi.check(_capi.lib().cusat_ldpc_decoder_set_max_ctas(self._h, max_ctas))
 
-    def frames_per_cta(self):
-        """2 when this decoder runs frame pairs (short frames, no learned
-        weights), else 1."""
-        n = _capi.lib().cusat_ldpc_decoder_frames_per_cta(self._h)
+    def set_frames_per_cta(self, n):
+        """0: by batch size (frame pairs once every SM receives one), 1: one
+        frame per CTA, 2: frame pairs whenever the code allows them."""
+        _capi.check(_capi.lib().cusat_ldpc_decoder_set_frames_per_cta(self._h, n))
+
+    def frames_per_cta(self, batch_size):
+        """Frames per CTA a launch of batch_size frames runs: 2 for frame
+        pairs (short frames, no learned weights), else 1."""
+        n = _capi.lib().cusat_ldpc_decoder_frames_per_cta(self._h, batch_size)
         _capi.check(min(n, 0))
         return n
 
@@ -343,6 +348,10 @@ class rx_fec:
 
     def capped_llr_gain(self, llr_gain):
         return float(_capi.lib().cusat_rx_fec_capped_llr_gain(self._h, llr_gain))
+
+    def set_frames_per_cta(self, n):
+        """As ldpc_decode_cuda.set_frames_per_cta."""
+        _capi.check(_capi.lib().cusat_rx_fec_set_frames_per_cta(self._h, n))
 
     def set_weights(self, weights):
         """Learned min-sum weights ([n_iter, 32, 2] int16 {beta, alpha/64}) or None."""

@@ -20,7 +20,9 @@ _SIGS = {
                                                   ctypes.POINTER(ctypes.c_void_p)]),
     "cusat_ldpc_decoder_destroy": (None, [ctypes.c_void_p]),
     "cusat_ldpc_decoder_info": (ctypes.c_int, [ctypes.c_void_p, _c_int_p]),
-    "cusat_ldpc_decoder_frames_per_cta": (ctypes.c_int, [ctypes.c_void_p]),
+    "cusat_ldpc_decoder_frames_per_cta": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_ldpc_decoder_set_frames_per_cta": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "cusat_rx_fec_set_frames_per_cta": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cusat_ldpc_decoder_set_weights": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "cusat_ldpc_decoder_set_max_ctas": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cusat_ldpc_decode_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,

@@ -45,6 +45,8 @@ struct Engine {
     cusat::DecodeArgs pair_layout{};  // its shared-memory carve-up and message stride
     int pair_grid_max = 0;
     int* list = nullptr;              // [max_batch] frames left to the one-frame kernel
+    int pair_mode = 0;                // 0 by batch size, 1 one frame per CTA, 2 pairs when the code allows
+    int sms = 0;
 
     int set_weights(const int16_t* w, int n_iter)
     {
@@ -83,7 +85,7 @@ struct Engine {
         proto.max_trials = max_trials;
         proto.syn_period = cusat::syndrome_period();
         cusat::decoder_smem_layout(&proto, cusat::smem_dims_of(proto.code, p->lanes));
-        int optin = 0, sms = 0;
+        int optin = 0;
         CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
         if (proto.sm_total > optin)
@@ -132,12 +134,26 @@ struct Engine {
         return CUSAT_OK;
     }
 
-    int frames_per_cta() const { return pair_fn && !proto.code.weights ? 2 : 1; }
+    // Frames per CTA of a launch of `batch` frames.  By default pairs run
+    // where they were measured faster on GB300: codes of at most 5
+    // circulant slots per layer (16-43 % more throughput once the SMs are
+    // busy), in launches whose pairs occupy at least three quarters of the
+    // SMs (a smaller launch would leave SMs idle that single frames fill).
+    // The wider short codes gain at most 13 % at four frames per SM and
+    // lose up to 35 % elsewhere: one frame per CTA unless asked.
+    int frames_per_cta(int batch) const
+    {
+        if (!pair_fn || proto.code.weights || pair_mode == 1)
+            return 1;
+        if (pair_mode == 2)
+            return 2;
+        return plan->cmax <= 5 && 4 * ((batch + 1) / 2) >= 3 * sms ? 2 : 1;
+    }
 
     int launch(cusat::DecodeArgs a, int batch, cudaStream_t stream)
     {
         a.n_frames = batch;
-        if (pair_fn && !a.code.weights) {
+        if (frames_per_cta(batch) == 2) {
             // frame pairs, then the one-frame kernel over the frames they
             // listed (usually none: its CTAs exit at once)
             cusat::DecodeArgs b = a;
@@ -293,11 +309,19 @@ int cusat_ldpc_decoder_set_max_ctas(cusat_ldpc_decoder* d, int max_ctas)
     return CUSAT_OK;
 }
 
-int cusat_ldpc_decoder_frames_per_cta(const cusat_ldpc_decoder* d)
+int cusat_ldpc_decoder_set_frames_per_cta(cusat_ldpc_decoder* d, int n)
 {
-    if (!d)
-        return fail(CUSAT_ERR_ARG, "null decoder");
-    return d->eng.frames_per_cta();
+    if (!d || n < 0 || n > 2)
+        return fail(CUSAT_ERR_ARG, "null decoder or frames per CTA outside 0..2");
+    d->eng.pair_mode = n;
+    return CUSAT_OK;
+}
+
+int cusat_ldpc_decoder_frames_per_cta(const cusat_ldpc_decoder* d, int batch)
+{
+    if (!d || batch <= 0)
+        return fail(CUSAT_ERR_ARG, "null decoder or empty batch");
+    return d->eng.frames_per_cta(batch);
 }
 
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* d, int32_t* out)
@@ -610,6 +634,14 @@ int cusat_rx_fec_set_weights(cusat_rx_fec* r, const int16_t* weights, int n_iter
     if (!r)
         return fail(CUSAT_ERR_ARG, "null chain");
     return r->eng.set_weights(weights, n_iter);
+}
+
+int cusat_rx_fec_set_frames_per_cta(cusat_rx_fec* r, int n)
+{
+    if (!r || n < 0 || n > 2)
+        return fail(CUSAT_ERR_ARG, "null chain or frames per CTA outside 0..2");
+    r->eng.pair_mode = n;
+    return CUSAT_OK;
 }
 
 int cusat_rx_fec_info(const cusat_rx_fec* r, int32_t* out)

@@ -60,12 +60,19 @@ void cusat_ldpc_decoder_destroy(cusat_ldpc_decoder* dec);
  * lanes (2 = paired-layer schedule) */
 int cusat_ldpc_decoder_info(const cusat_ldpc_decoder* dec, int32_t* out);
 
-/* Frames one CTA of this decoder holds: 2 when it decodes frame pairs (codes
- * decoded one layer per step whose pair fits twice per SM -- the short
- * frames -- without learned weights; frames with channel LLRs beyond the
- * saturation-free range then go to a one-frame launch), else 1.  Results do
- * not depend on it. */
-int cusat_ldpc_decoder_frames_per_cta(const cusat_ldpc_decoder* dec);
+/* Frames per CTA.  Codes decoded one layer per step whose frame pair fits
+ * twice per SM (the short frames) can run two frames per CTA when no
+ * learned weights are set; frames with channel LLRs beyond the
+ * saturation-free range then go to a one-frame launch.  n = 0 (default):
+ * pairs for codes of at most 5 circulants per layer (short rates 1/4 to
+ * 1/2) in launches whose pairs occupy three quarters of the SMs or more;
+ * 1: one frame per CTA; 2: pairs whenever the code allows -- for smaller
+ * launches of those codes that overlap others on several streams (the
+ * wider short codes measured slower as pairs).  Results do not depend on
+ * it.  cusat_ldpc_decoder_frames_per_cta returns what a launch of `batch`
+ * frames runs (1 or 2). */
+int cusat_ldpc_decoder_set_frames_per_cta(cusat_ldpc_decoder* dec, int n);
+int cusat_ldpc_decoder_frames_per_cta(const cusat_ldpc_decoder* dec, int batch);
 
 /* Learned min-sum weights (no counterpart in the reference, whose
  * normalised-min-sum hook nms_scale, ldpc_decode_kernel.cu:75-90, is never
@@ -197,6 +204,8 @@ void cusat_rx_fec_destroy(cusat_rx_fec* rx);
 int cusat_rx_fec_info(const cusat_rx_fec* rx, int32_t* out);
 /* Learned weights for the chain's decoder (see cusat_ldpc_decoder_set_weights). */
 int cusat_rx_fec_set_weights(cusat_rx_fec* rx, const int16_t* weights, int n_iter);
+/* The decoder's frames per CTA, as cusat_ldpc_decoder_set_frames_per_cta. */
+int cusat_rx_fec_set_frames_per_cta(cusat_rx_fec* rx, int n);
 float cusat_rx_fec_capped_llr_gain(const cusat_rx_fec* rx, float llr_gain);
 /* Symbols on the device in, results to device or mapped pinned memory;
  * llr_gain is capped like demap_batch does (demapper_kernel.cu:283-291).

@@ -68,7 +68,8 @@ def test_pairs_match_oracle_every_class(cuda, rate):
     torch = cuda
     T = 30
     dec = cs.ldpc_decode_cuda(SHORT, rate, T, 96)
-    assert dec.frames_per_cta() == 2
+    dec.set_frames_per_cta(2)
+    assert dec.frames_per_cta(1) == 2
     llr = _llr(SHORT, rate, 96, seed=700 + rate)
     ho, to = O.ldpc_decode(SHORT, rate, llr, T, nthreads=THREADS)
     # odd and even batches: a CTA of an odd batch keeps one slot empty
@@ -91,6 +92,7 @@ def test_pairs_refill_and_saturating_list(cuda, rate):
     llr[1::4, ::13] = np.where(llr[1::4, ::13] < 0, -32768, 32767)
     ho, to = O.ldpc_decode(SHORT, rate, llr, T, nthreads=THREADS)
     dec = cs.ldpc_decode_cuda(SHORT, rate, T, B)
+    dec.set_frames_per_cta(2)
     dec.set_max_ctas(3)
     for rep in range(2):
         h, t = _decode(torch, dec, llr, T)
@@ -122,6 +124,7 @@ def test_pairs_trial_cap_edges(cuda):
     both = np.concatenate([llr, clean])
     for T in (0, 1, 2):
         dec = cs.ldpc_decode_cuda(SHORT, rate, T, len(both))
+        dec.set_frames_per_cta(2)
         ho, to = O.ldpc_decode(SHORT, rate, both, T, nthreads=THREADS)
         h, t = _decode(torch, dec, both, T)
         _same(f"T={T}", h, t, ho, to)
@@ -133,26 +136,60 @@ def test_learned_weights_keep_one_frame_kernel(cuda):
     rate = E.RATE_1_2
     T = 20
     dec = cs.ldpc_decode_cuda(SHORT, rate, T, 32)
-    assert dec.frames_per_cta() == 2
+    dec.set_frames_per_cta(2)
+    assert dec.frames_per_cta(32) == 2
     w = np.zeros((T, 32, 2), np.int16)
     w[:, :, 0] = 1
     w[:, :, 1] = 48  # beta 1, alpha 0.75
     dec.set_weights(w)
-    assert dec.frames_per_cta() == 1
+    assert dec.frames_per_cta(32) == 1
     llr = _llr(SHORT, rate, 32, seed=77)
     ho, to = O.ldpc_decode(SHORT, rate, llr, T, weights=w, nthreads=THREADS)
     h, t = _decode(torch, dec, llr, T)
     _same("weighted", h, t, ho, to)
     dec.set_weights(None)
-    assert dec.frames_per_cta() == 2
+    assert dec.frames_per_cta(32) == 2
     ho, to = O.ldpc_decode(SHORT, rate, llr, T, nthreads=THREADS)
     h, t = _decode(torch, dec, llr, T)
     _same("plain again", h, t, ho, to)
 
 
-def test_normal_frames_stay_one_per_cta(cuda):
-    assert cs.ldpc_decode_cuda(E.FECFRAME_NORMAL, E.RATE_3_5, 10, 8).frames_per_cta() == 1
-    assert cs.ldpc_decode_cuda(E.FECFRAME_NORMAL, E.RATE_22_30, 10, 8).frames_per_cta() == 1
+def test_frames_per_cta_choice(cuda):
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for fs, rate in ((E.FECFRAME_NORMAL, E.RATE_3_5), (E.FECFRAME_NORMAL, E.RATE_22_30)):
+        dec = cs.ldpc_decode_cuda(fs, rate, 10, 8)
+        dec.set_frames_per_cta(2)
+        assert dec.frames_per_cta(8) == 1  # normal frames: no pair fits
+    dec = cs.ldpc_decode_cuda(SHORT, E.RATE_1_2, 10, 4 * sms)
+    lo = -(-3 * sms // 4) * 2  # the smallest batch whose pairs cover 3/4 of the SMs
+    assert dec.frames_per_cta(lo - 2) == 1 and dec.frames_per_cta(lo) == 2
+    wide = cs.ldpc_decode_cuda(SHORT, E.RATE_8_9, 10, 4 * sms)
+    assert wide.frames_per_cta(4 * sms) == 1  # 28 slots: one frame per CTA by default
+    wide.set_frames_per_cta(2)
+    assert wide.frames_per_cta(1) == 2
+    dec.set_frames_per_cta(1)
+    assert dec.frames_per_cta(4 * sms) == 1
+    dec.set_frames_per_cta(2)
+    assert dec.frames_per_cta(1) == 2
+    with pytest.raises(cs.CusatError):
+        dec.set_frames_per_cta(3)
+
+
+def test_pairs_by_batch_size_match_oracle(cuda):
+    """Default choice: a small batch runs one frame per CTA, a batch whose
+    pairs cover the SMs frame pairs -- same results."""
+    torch = cuda
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rate, T = E.RATE_1_2, 25
+    B = 2 * sms + 3
+    llr = _llr(SHORT, rate, B, seed=4242)
+    ho, to = O.ldpc_decode(SHORT, rate, llr, T, nthreads=THREADS)
+    dec = cs.ldpc_decode_cuda(SHORT, rate, T, B)
+    assert dec.frames_per_cta(B) == 2 and dec.frames_per_cta(40) == 1
+    for n in (B, 40):
+        h, t = _decode(torch, dec, llr[:n], T)
+        _same(f"B={n} ({dec.frames_per_cta(n)} per CTA)", h, t, ho[:n], to[:n])
 
 
 _PERIOD_CHILD = r"""
@@ -167,6 +204,7 @@ for fs, rate in ((E.FECFRAME_SHORT, E.RATE_1_2), (E.FECFRAME_SHORT, E.RATE_5_6),
     llr = _llr(fs, rate, 24, seed=31 + rate)
     ho, to = O.ldpc_decode(fs, rate, llr, 25, nthreads=8, syn_period=3)
     dec = cs.ldpc_decode_cuda(fs, rate, 25, 24)
+    dec.set_frames_per_cta(2)
     h, t = _decode(torch, dec, llr, 25)
     _same(f"period 3 fs {{fs}} rate {{rate}}", h, t, ho, to)
 print("ok")
