@@ -19,13 +19,13 @@ constexpr int kBig = 1 << 20;      // |extrinsic| of an absent edge
 
 // Where the next step's message rows wait: shared memory (per-thread
 // asynchronous copies) or registers (loads one step ahead).  Measured per
-// kernel class on GB300: shared memory wins only for 9 slots x 2 lanes; the
-// other classes lose more L1 (their register spills live there) than they
-// gain in registers.
+// kernel class on GB300: shared memory wins only for 8 and 9 slots x 2
+// lanes; the other classes lose more L1 (their register spills live there)
+// than they gain in registers.
 #ifdef __CUDACC__
 __host__ __device__
 #endif
-constexpr bool stage_rows_in_smem(int cmax, int lanes) { return cmax == 9 && lanes == 2; }
+constexpr bool stage_rows_in_smem(int cmax, int lanes) { return (cmax == 8 || cmax == 9) && lanes == 2; }
 
 // Slot descriptor of one (layer, circulant slot), uint4:
 //   x = byte offset in shared memory of the circulant's first bit

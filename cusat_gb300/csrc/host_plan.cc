@@ -26,7 +26,10 @@ namespace cusat {
 
 int cmax_bucket(int cnt_max)
 {
-    static const int buckets[] = {3, 5, 9, 14, 20, 28};
+    // one kernel instantiation per bucket: with packed pairs of edges a
+    // check row of cmax + 2 slots wastes at most one half (an absent slot
+    // or the pad), the common DVB-S2 codes fit exactly
+    static const int buckets[] = {2, 3, 4, 5, 6, 8, 9, 10, 12, 14, 16, 18, 20, 26, 28};
     for (int b : buckets)
         if (cnt_max <= b)
             return b;

@@ -1,9 +1,9 @@
-// Instantiations and launch helpers of the layered decoder kernel.
+// Instantiations and launch helpers of the layered decoder kernel (one
+// frame per CTA).
 #include <stdlib.h>
 
 #include "kernels.h"
 #include "ldpc_kernel.cuh"
-#include "ldpc_pair.cuh"
 
 namespace cusat {
 
@@ -22,34 +22,26 @@ int align16(int x) { return (x + 15) & ~15; }
 const void* select_decoder_kernel(int cmax, int lanes)
 {
     switch (cmax) {
+    case 2: return pick<2>(lanes);
     case 3: return pick<3>(lanes);
+    case 4: return pick<4>(lanes);
     case 5: return pick<5>(lanes);
+    case 6: return pick<6>(lanes);
+    case 8: return pick<8>(lanes);
     case 9: return pick<9>(lanes);
+    case 10: return pick<10>(lanes);
+    case 12: return pick<12>(lanes);
     case 14: return pick<14>(lanes);
+    case 16: return pick<16>(lanes);
+    case 18: return pick<18>(lanes);
     case 20: return pick<20>(lanes);
+    case 26: return pick<26>(lanes);
     case 28: return pick<28>(lanes);
     default: return nullptr;
     }
 }
 
 int decoder_threads(int lanes) { return lanes * lane_threads(lanes); }
-
-static_assert(kPairThreads == lane_threads(1), "the frame-pair kernel runs one lane");
-
-const void* select_pair_kernel(int cmax)
-{
-    switch (cmax) {
-    case 3: return (const void*)ldpc_pair_kernel<3>;
-    case 5: return (const void*)ldpc_pair_kernel<5>;
-    case 9: return (const void*)ldpc_pair_kernel<9>;
-    case 14: return (const void*)ldpc_pair_kernel<14>;
-    case 20: return (const void*)ldpc_pair_kernel<20>;
-    case 28: return (const void*)ldpc_pair_kernel<28>;
-    default: return nullptr;
-    }
-}
-
-int pair_msg_row(int cmax) { return (2 * (cmax + 2) + 15) / 16 * 16; }
 
 int syndrome_period()
 {
@@ -81,28 +73,6 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     const int rw = (d.cmax + 2 + 15) / 16;
     take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * lane_threads(d.lanes) * rw * 16 : 0);
     a->sm_total = off;
-}
-
-void pair_smem_layout(DecodeArgs* a, const SmemDims& d, int max_stage)
-{
-    int off = align16(d.N * 4);  // APP words: frame A's int16 in the low half, B's in the high half
-    auto take = [&](int* field, int bytes) {
-        *field = off;
-        off = align16(off + bytes);
-    };
-    take(&a->sm_dummy, 2 * kM * 4);  // +32640 region, then the junk region
-    take(&a->sm_stage, kStageSets * max_stage * kM * 4);
-    take(&a->sm_tab, d.q * d.cmax * 16);
-    take(&a->sm_cnt, d.q);
-    take(&a->sm_sched, d.n_steps * 4);
-    take(&a->sm_conf, d.n_steps);
-    take(&a->sm_item_off, (d.n_steps + 1) * 2);
-    take(&a->sm_items, d.n_items * 8);
-    take(&a->sm_code, (int)sizeof(DevCode));
-    take(&a->sm_misc, (int)sizeof(PairState));
-    take(&a->sm_msgbuf, 0);
-    a->sm_total = off;
-    a->max_stage = max_stage;
 }
 
 SmemDims smem_dims_of(const DevCode& c, int lanes)

@@ -129,7 +129,9 @@ def test_mixed_batch_equals_single_modcod(mixed):
     b = cs.batch(_modcod_triples(per), max_trials=T, max_frames=64)
     n_modcods, n_classes, max_frames, max_trials = b.info()
     assert (n_modcods, max_frames, max_trials) == (len(per), 64, T)
-    assert n_classes == 6
+    # one class per kernel instantiation (circulant-slot bucket, lanes)
+    assert n_classes == len({(cs.code_info(fs, rate)["cmax"], cs.code_info(fs, rate)["lanes"])
+                             for _, rate, fs in _modcod_triples(per)})
     bufs, frames = _buffers(per, order, torch)
     b.launch(frames, torch.cuda.current_stream())
     torch.cuda.synchronize()

@@ -150,13 +150,21 @@ def test_bench_mixed_batch_matches_oracle(cuda):
 
 # one code per decoder kernel class (circulant slots per layer, lanes)
 CLASS_CODES = [
-    (NORMAL, E.RATE_1_4), (SHORT, E.RATE_1_4),      # 3 slots
-    (NORMAL, E.RATE_1_2), (SHORT, E.RATE_1_2),      # 5
-    (NORMAL, E.RATE_3_5), (SHORT, E.RATE_3_5),      # 9
-    (NORMAL, E.RATE_3_4), (SHORT, E.RATE_3_4),      # 14
-    (NORMAL, E.RATE_5_6), (SHORT, E.RATE_5_6),      # 20
-    (NORMAL, E.RATE_22_30),                         # 20, one lane (sequential schedule)
-    (NORMAL, E.RATE_9_10), (SHORT, E.RATE_8_9),     # 28
+    (NORMAL, E.RATE_1_4), (SHORT, E.RATE_1_4),          # 2 slots
+    (NORMAL, E.RATE_1_3), (SHORT, E.RATE_1_3),          # 3
+    (NORMAL, E.RATE_2_5), (SHORT, E.RATE_2_5),          # 4
+    (NORMAL, E.RATE_1_2), (SHORT, E.RATE_1_2),          # 5
+    (NORMAL, E.RATE_90_180),                            # 6
+    (NORMAL, E.RATE_2_3), (SHORT, E.RATE_2_3),          # 8
+    (NORMAL, E.RATE_3_5), (SHORT, E.RATE_3_5),          # 9
+    (NORMAL, E.RATE_116_180),                           # 10
+    (NORMAL, E.RATE_3_4), (SHORT, E.RATE_3_4),          # 12
+    (NORMAL, E.RATE_128_180),                           # 14
+    (NORMAL, E.RATE_4_5), (NORMAL, E.RATE_22_30),       # 16, two lanes and one lane (sequential schedule)
+    (NORMAL, E.RATE_140_180), (SHORT, E.RATE_5_6),      # 18
+    (NORMAL, E.RATE_5_6),                               # 20
+    (NORMAL, E.RATE_8_9), (SHORT, E.RATE_8_9),          # 26
+    (NORMAL, E.RATE_9_10),                              # 28
 ]
 
 
