@@ -678,20 +678,31 @@ __device__ __forceinline__ int load_llr(const DevCode& c, int16_t* app, const in
             }
             *reinterpret_cast<uint4*>(app + v) = make_uint4(o[0], o[1], o[2], o[3]);
         }
+        // Parity bits p and p + 8 land 8 layers apart, in one shared-memory
+        // bank: the threads of a warp store their 8 values in rotated order
+        // (thread t starts at value t mod 8), so one store instruction of
+        // the warp spreads over the banks instead of hitting one 32 times.
+        const int rot = threadIdx.x & 7;
         for (int p = threadIdx.x * 8; p < R; p += blockDim.x * 8) {
             const uint4 w = __ldcs(reinterpret_cast<const uint4*>(src + K + p));
-            const uint32_t in[4] = {w.x, w.y, w.z, w.w};
-            int li = p % q, lj = p / q;
+            const int li0 = p % q, lj0 = p / q;
 #pragma unroll
-            for (int k = 0; k < 8; k++) {
-                int x = (int)(int16_t)(in[k >> 1] >> (16 * (k & 1)));
+            for (int s = 0; s < 8; s++) {
+                const int k = (s + rot) & 7;
+                const uint32_t wd = k < 2 ? w.x : k < 4 ? w.y : k < 6 ? w.z : w.w;
+                int x = (int)(int16_t)(wd >> (16 * (k & 1)));
                 x = max(x, -32767);
                 over |= abs(x) > lim;
-                app[K + li * kM + lj] = (int16_t)x;
-                if (++li == q) {
-                    li = 0;
+                int li = li0 + k, lj = lj0;  // q >= 5: at most two wraps
+                if (li >= q) {
+                    li -= q;
                     lj++;
                 }
+                if (li >= q) {
+                    li -= q;
+                    lj++;
+                }
+                app[K + li * kM + lj] = (int16_t)x;
             }
         }
     } else {
