@@ -217,28 +217,21 @@ __device__ __forceinline__ int load_llr_pair(const DevCode& c, int16_t* app16, i
                 app16[2 * (v + k) + half] = (int16_t)x;
             }
         }
-        // stores in rotated order, as in the one-frame load (parity bits p
-        // and p + 8 land 8 layers apart, in one bank)
-        const int rot = threadIdx.x & 7;
+        // plain order: the rotated stores of the one-frame load cost this
+        // kernel registers (57 -> 80) and measured slower here
         for (int p = threadIdx.x * 8; p < R; p += blockDim.x * 8) {
             const uint4 w = __ldcs(reinterpret_cast<const uint4*>(src + K + p));
-            const int li0 = p % q, lj0 = p / q;
+            const uint32_t in[4] = {w.x, w.y, w.z, w.w};
+            int li = p % q, lj = p / q;
 #pragma unroll
-            for (int s = 0; s < 8; s++) {
-                const int k = (s + rot) & 7;
-                const uint32_t wd = k < 2 ? w.x : k < 4 ? w.y : k < 6 ? w.z : w.w;
-                const int x = max((int)(int16_t)(wd >> (16 * (k & 1))), -32767);
+            for (int k = 0; k < 8; k++) {
+                const int x = max((int)(int16_t)(in[k >> 1] >> (16 * (k & 1))), -32767);
                 over |= abs(x) > lim;
-                int li = li0 + k, lj = lj0;  // q >= 5: at most two wraps
-                if (li >= q) {
-                    li -= q;
-                    lj++;
-                }
-                if (li >= q) {
-                    li -= q;
-                    lj++;
-                }
                 app16[2 * (K + li * kM + lj) + half] = (int16_t)x;
+                if (++li == q) {
+                    li = 0;
+                    lj++;
+                }
             }
         }
     } else {
