@@ -67,7 +67,7 @@ struct DecodeArgs {
     uint8_t* hard;           // single code: [n_frames][K/8]
     int32_t* trials;         // single code: [n_frames]
     uint4* msg;              // [gridDim.x][msg_stride] scratch
-    int msg_stride;          // uint4 per CTA: max over the launch's codes of R * msg_row / 16
+    int msg_stride;          // uint4 per CTA: max over the launch's codes of R * row bytes / 16
     unsigned int* queue;     // [0] frame counter, [1] CTAs done: zero at launch, zeroed again by the last CTA
     // Frame lists between the frame-pair kernel and the one-frame kernel
     // (single code): the pair kernel appends the frames that need the
@@ -128,6 +128,50 @@ __device__ __forceinline__ void load_row(uint4 (&dst)[RW], const uint4* src, boo
 #pragma unroll
     for (int w = 0; w < RW; w++)
         dst[w] = pred ? __ldcg(src + w) : make_uint4(0, 0, 0, 0);
+}
+
+// Message rows of the one-frame kernel: W 32-bit words per check row
+// (row_words: 4, 8, 16 or 32 bytes, the edge count rounded up), moved with
+// one load or store of that width (two 128-bit ones for 32 bytes).
+template <int W>
+__device__ __forceinline__ int row_byte_w(const uint32_t (&row)[W], int e)
+{
+    return sbyte(row[e >> 2], e & 3);
+}
+
+template <int W>
+__device__ __forceinline__ void load_row_w(uint32_t (&dst)[W], const uint32_t* src, bool pred)
+{
+    if constexpr (W == 1) {
+        dst[0] = pred ? __ldcg(src) : 0u;
+    } else if constexpr (W == 2) {
+        const uint2 v = pred ? __ldcg(reinterpret_cast<const uint2*>(src)) : make_uint2(0, 0);
+        dst[0] = v.x;
+        dst[1] = v.y;
+    } else {
+#pragma unroll
+        for (int k = 0; k < W / 4; k++) {
+            const uint4 v = pred ? __ldcg(reinterpret_cast<const uint4*>(src) + k) : make_uint4(0, 0, 0, 0);
+            dst[4 * k] = v.x;
+            dst[4 * k + 1] = v.y;
+            dst[4 * k + 2] = v.z;
+            dst[4 * k + 3] = v.w;
+        }
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void store_row_w(uint32_t* dst, const uint32_t (&v)[W])
+{
+    if constexpr (W == 1) {
+        __stcg(dst, v[0]);
+    } else if constexpr (W == 2) {
+        __stcg(reinterpret_cast<uint2*>(dst), make_uint2(v[0], v[1]));
+    } else {
+#pragma unroll
+        for (int k = 0; k < W / 4; k++)
+            __stcg(reinterpret_cast<uint4*>(dst) + k, make_uint4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
+    }
 }
 
 // Message rows of the next step are staged in shared memory by per-thread
@@ -243,10 +287,10 @@ __device__ __forceinline__ int scaled_mag(int r, int beta, int alpha)
 // One check row of one layer: gather, offset min-sum, scatter, new message
 // row; straight-line code for every layer (plain, staged and absent slots
 // differ only in their descriptors).
-template <int CMAX, int RW, bool SAT>
+template <int CMAX, int W, bool SAT>
 __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char* smem, const uint4* tb, int cnt,
-                                              int j, int ps0, int ps1, bool absent, const uint4 (&cur)[RW],
-                                              uint4* dst, int trial)
+                                              int j, int ps0, int ps1, bool absent, const uint32_t (&cur)[W],
+                                              uint32_t* dst, int trial)
 {
     constexpr int NE = CMAX + 2;
     // Wide rows would not fit the register budget with every slot's store
@@ -261,8 +305,8 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
     const int a0 = lds16(smem, ps0);
     const int a1 = lds16(smem, ps1);
     {
-        const int x0 = madd(row_byte(cur, 0), neg, a0);
-        const int x1 = madd(row_byte(cur, 1), neg, a1);
+        const int x0 = madd(row_byte_w(cur, 0), neg, a0);
+        const int x1 = madd(row_byte_w(cur, 1), neg, a1);
         d[0] = SAT ? sat16(x0) : x0;
         d[1] = absent ? kBig : (SAT ? sat16(x1) : x1);
     }
@@ -272,7 +316,7 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
         const int ad = madd(rot720(j2, w.y, one), one, (int)w.x);
         if (kKeepAddr)
             sa[e] = madd((int)w.z, one, ad);
-        const int x = madd(row_byte(cur, e + 2), neg, lds16(smem, ad));
+        const int x = madd(row_byte_w(cur, e + 2), neg, lds16(smem, ad));
         d[2 + e] = SAT ? sat16(x) : x;
     }
     // check node: min1/min2 of |extrinsic|, sign product
@@ -301,9 +345,9 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
     const int sg = sx >> 31;
     const int p1 = madd(sg, neg, m1 ^ sg), p2 = madd(sg, neg, m2 ^ sg);
     const int dp = p1 - p2, nr1 = -r1, two = one + one;
-    uint32_t wv[RW * 4];
+    uint32_t wv[W];
 #pragma unroll
-    for (int k = 0; k < RW * 4; k++)
+    for (int k = 0; k < W; k++)
         wv[k] = 0;
 #pragma unroll
     for (int e = 0; e < NE; e++) {
@@ -328,7 +372,7 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
                 // re-read the APP (unchanged: no other check of the step
                 // writes this bit); a staged slot stores its delta, the
                 // completion saturates the sum once
-                const int delta = mg - row_byte(cur, e);
+                const int delta = mg - row_byte_w(cur, e);
                 v = tb[e - 2].z == 0 ? sat16(lds16(smem, at) + delta) : delta;
             } else {
                 v = madd(mg, one, d[e]);
@@ -336,9 +380,7 @@ __device__ __forceinline__ void process_check(const int16_t* wts, unsigned char*
             sts16(smem, at, v);
         }
     }
-#pragma unroll
-    for (int w = 0; w < RW; w++)
-        __stcg(dst + w, make_uint4(wv[4 * w], wv[4 * w + 1], wv[4 * w + 2], wv[4 * w + 3]));
+    store_row_w<W>(dst, wv);
 }
 
 // ---------------------------------------------------------------------------
@@ -418,10 +460,10 @@ __device__ __forceinline__ int ldu16(const unsigned char* smem, int off)
     return *reinterpret_cast<const uint16_t*>(smem + off);
 }
 
-template <int CMAX, int RW, bool WTS>
+template <int CMAX, int W, bool WTS>
 __device__ __forceinline__ void process_check_packed(const int16_t* wts, unsigned char* smem, const uint4* tb, int cnt,
                                                      int j, int ps0, int ps1r, int ps1w, bool absent,
-                                                     const uint4 (&cur)[RW], uint4* dst, int trial)
+                                                     const uint32_t (&cur)[W], uint32_t* dst, int trial)
 {
     constexpr int NE = CMAX + 2;
     constexpr int NP = (NE + 1) / 2;
@@ -433,7 +475,7 @@ __device__ __forceinline__ void process_check_packed(const int16_t* wts, unsigne
     // gather: x = APP + (-m_old) two edges at a time
     {
         const int a0 = ldu16(smem, ps0), a1 = ldu16(smem, ps1r);
-        x[0] = vadd2((uint32_t)madd(a1, k16, a0), prmt(cur[0].x, 0, pair_sel(0, false)));
+        x[0] = vadd2((uint32_t)madd(a1, k16, a0), prmt(cur[0], 0, pair_sel(0, false)));
     }
     int lo = 0;
 #pragma unroll
@@ -444,7 +486,7 @@ __device__ __forceinline__ void process_check_packed(const int16_t* wts, unsigne
         if (kKeepAddr)
             sa[c] = madd((int)w.z, one, ad);
         const int a = ldu16(smem, ad);
-        const uint32_t rw = word_of(cur[e >> 4], (e >> 2) & 3);
+        const uint32_t rw = cur[e >> 2];
         if ((e & 1) == 0) {
             lo = a;
             if (e == NE - 1)  // odd edge count: the high half is a pad that never wins a minimum
@@ -514,13 +556,11 @@ __device__ __forceinline__ void process_check_packed(const int16_t* wts, unsigne
         }
     }
     // new message row: byte e = -message of edge e
-    uint32_t wv[RW * 4];
+    uint32_t wv[W];
 #pragma unroll
-    for (int q = 0; q < RW * 4; q++)
+    for (int q = 0; q < W; q++)
         wv[q] = 2 * q < NP ? prmt(nm[2 * q], 2 * q + 1 < NP ? nm[2 * q + 1] : 0u, 0x6420) : 0u;
-#pragma unroll
-    for (int q = 0; q < RW; q++)
-        __stcg(dst + q, make_uint4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]));
+    store_row_w<W>(dst, wv);
 }
 
 // Completion of step s's shared groups: thread j of each lane takes bit j of
@@ -558,8 +598,7 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
                              const SmemCode& t, const Job& job)
 {
     constexpr bool SAT = MODE == 0;
-    constexpr int NE = CMAX + 2;
-    constexpr int RW = (NE + 15) / 16;
+    constexpr int W = row_words(CMAX);
     const int tid = threadIdx.x;
     constexpr int LT = lane_threads(LANES);
     const int lane = (LANES == 2 && tid >= LT) ? 1 : 0;
@@ -569,25 +608,26 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
     const int period = a.syn_period > 1 ? a.syn_period : 1;
     const int pty = 2 * K;         // byte offset of the parity APP
     const int spare = 2 * c.N;     // scratch slot for the absent parity edge
-    uint4* msg_cta = a.msg + (size_t)blockIdx.x * (size_t)a.msg_stride;
+    uint32_t* msg_cta = reinterpret_cast<uint32_t*>(a.msg + (size_t)blockIdx.x * (size_t)a.msg_stride);
     constexpr bool kSmemRows = stage_rows_in_smem(CMAX, LANES);
+    static_assert(!kSmemRows || W == 4, "rows staged in shared memory are 16 bytes");
     // staged rows (kSmemRows): set s & 1 holds this thread's row of step s
-    uint4* mrow = reinterpret_cast<uint4*>(smem + a.sm_msgbuf) + (size_t)tid * RW;
-    const int mset = (int)blockDim.x * RW;
+    uint4* mrow = reinterpret_cast<uint4*>(smem + a.sm_msgbuf) + tid;
+    const int mset = (int)blockDim.x;
     int result = -1;
 
     for (int trial = 0;; trial++) {
         // step 0's rows are requested before the syndrome pass so that their
         // latency hides behind it (left unread when the frame converged)
         const bool load = trial > 0 && trial < T;
-        uint4 cur[RW];
+        uint32_t cur[W];
         {
             const int i0 = t.sched[lane];
-            const uint4* src = msg_cta + ((size_t)max(i0, 0) * kM + j) * RW;
+            const uint32_t* src = msg_cta + ((size_t)max(i0, 0) * kM + j) * W;
             if (kSmemRows)
-                stage_row_async<RW>(mrow, src, load && active && i0 >= 0);
+                stage_row_async<1>(mrow, reinterpret_cast<const uint4*>(src), load && active && i0 >= 0);
             else
-                load_row<RW>(cur, src, load && active && i0 >= 0);
+                load_row_w<W>(cur, src, load && active && i0 >= 0);
         }
         // periodic + final check (reference ldpc_decode_kernel.cu:693-694)
         if ((period == 1 || trial % period == 0 || trial == T) &&
@@ -599,20 +639,23 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
             break;
         for (int s = 0; s < n_steps; s++) {
             const int i = t.sched[2 * s + lane];
-            uint4 nxt[RW];
+            uint32_t nxt[W];
             {
                 const int i_n = s + 1 < n_steps ? t.sched[2 * (s + 1) + lane] : -1;
-                const uint4* src = msg_cta + ((size_t)max(i_n, 0) * kM + j) * RW;
+                const uint32_t* src = msg_cta + ((size_t)max(i_n, 0) * kM + j) * W;
                 if (kSmemRows)
-                    stage_row_async<RW>(mrow + ((s + 1) & 1) * mset, src, load && active && i_n >= 0);
+                    stage_row_async<1>(mrow + ((s + 1) & 1) * mset, reinterpret_cast<const uint4*>(src),
+                                       load && active && i_n >= 0);
                 else
-                    load_row<RW>(nxt, src, load && active && i_n >= 0);
+                    load_row_w<W>(nxt, src, load && active && i_n >= 0);
             }
             if (kSmemRows) {
                 wait_staged_but_last();
+                const uint4 m = (load && active && i >= 0) ? mrow[(s & 1) * mset] : make_uint4(0, 0, 0, 0);
+                const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
 #pragma unroll
-                for (int w = 0; w < RW; w++)
-                    cur[w] = (load && active && i >= 0) ? mrow[(s & 1) * mset + w] : make_uint4(0, 0, 0, 0);
+                for (int w = 0; w < W; w++)
+                    cur[w] = mw[w & 3];
             }
             if (active) {
                 // groups of the previous step whose completion was deferred
@@ -621,16 +664,16 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
                 if (i >= 0) {
                     const int ps0 = pty + 2 * (i * kM + j);
                     const bool absent = (i == 0 && j == 0);
-                    uint4* dst = msg_cta + ((size_t)i * kM + j) * RW;
+                    uint32_t* dst = msg_cta + ((size_t)i * kM + j) * W;
                     if constexpr (SAT) {
                         const int ps1 = i > 0 ? ps0 - 2 * kM : (absent ? spare : pty + 2 * ((q - 1) * kM + j - 1));
-                        process_check<CMAX, RW, true>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent,
+                        process_check<CMAX, W, true>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0, ps1, absent,
                                                       cur, dst, trial);
                     } else {
                         // the absent edge reads the +32640 region and writes the junk region
                         const int ps1r = i > 0 ? ps0 - 2 * kM : (absent ? a.sm_dummy : pty + 2 * ((q - 1) * kM + j - 1));
                         const int ps1w = absent ? a.sm_dummy + 2 * kM : ps1r;
-                        process_check_packed<CMAX, RW, MODE == 2>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0,
+                        process_check_packed<CMAX, W, MODE == 2>(c.weights, smem, t.tab + i * CMAX, t.cnt[i], j, ps0,
                                                                   ps1r, ps1w, absent, cur, dst, trial);
                     }
                 }
@@ -643,7 +686,7 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
             __syncthreads();
             if (!kSmemRows) {
 #pragma unroll
-                for (int w = 0; w < RW; w++)
+                for (int w = 0; w < W; w++)
                     cur[w] = nxt[w];
             }
         }
