@@ -14,8 +14,8 @@
 // one add and one unsigned DPX min (viaddmin): consecutive threads read
 // consecutive halfwords, so gathers and scatters are conflict-free
 // shared-memory accesses.  Check-to-bit messages (int8) live in this CTA's
-// global scratch, one 16- or 32-byte row per check (the two parity edges,
-// then the circulants), loaded with 128-bit loads one step ahead of use.
+// global scratch, one row of 4, 8, 16 or 32 bytes per check (the two parity
+// edges, then the circulants; row_words), loaded one step ahead of use.
 //
 // Arithmetic.  The reference semantics (qsat16 extrinsic, offset min-sum
 // with beta 1, int8 clamp, saturating APP updates) are computed exactly.
