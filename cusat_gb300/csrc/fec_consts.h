@@ -28,14 +28,24 @@ __host__ __device__
 constexpr bool stage_rows_in_smem(int cmax, int lanes) { return (cmax == 8 || cmax == 9) && lanes == 2; }
 
 // 32-bit words of one check row of messages in the one-frame kernel: one
-// byte per edge (cmax + 2 edges), rounded up to 4, 8, 16 or 32 bytes so
-// that a row moves with one load or store.  The rows of a CTA stay in L2
-// (for normal rate 1/4, 48,600 checks: 4 bytes instead of 16, 30 instead of
-// 118 MB for 152 CTAs).
+// byte per edge (cmax + 2 edges), rounded up to 4, 8, 12, 16 or 32 bytes
+// (one load or store per row, three for 12), so that the rows of the
+// resident CTAs stay in L2 (normal rate 1/4, 48,600 checks: 4 bytes instead
+// of 16, 30 instead of 118 MB for 152 CTAs).  Rows staged in shared memory
+// stay 16 bytes: one 16-byte asynchronous copy; three 4-byte ones measured
+// 12 % slower on the 9-slot two-lane class.
 #ifdef __CUDACC__
 __host__ __device__
 #endif
-constexpr int row_words(int cmax) { return cmax + 2 <= 4 ? 1 : cmax + 2 <= 8 ? 2 : cmax + 2 <= 16 ? 4 : 8; }
+constexpr int row_words(int cmax, int lanes)
+{
+    return stage_rows_in_smem(cmax, lanes) ? 4
+           : cmax + 2 <= 4                 ? 1
+           : cmax + 2 <= 8                 ? 2
+           : cmax + 2 <= 12                ? 3
+           : cmax + 2 <= 16                ? 4
+                                           : 8;
+}
 
 // Slot descriptor of one (layer, circulant slot), uint4:
 //   x = byte offset in shared memory of the circulant's first bit

@@ -91,7 +91,6 @@ void build_plan(CodePlan& c, int framesize, int rate)
     c.cmax = cmax_bucket(c.cnt_max);
     if (c.cmax < 0)
         throw std::runtime_error("check degree above the largest kernel bucket");
-    c.msg_row = 4 * row_words(c.cmax);
     // no information bit of the frame may push |APP| past int16 when every
     // channel LLR is within fast_lim: |APP| <= |llr| + 127 * (deg + 1)
     c.fast_lim = 32767 - 127 * (c.dv_max + 2);
@@ -116,6 +115,7 @@ void build_plan(CodePlan& c, int framesize, int rate)
         }
         c.lanes = 1;
     }
+    c.msg_row = 4 * row_words(c.cmax, c.lanes);
 
     // Shared groups per step: a group (table row) reached by several
     // circulants of one step has its bits updated by all of them.  Each such

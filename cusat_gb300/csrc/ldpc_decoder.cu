@@ -70,8 +70,8 @@ void decoder_smem_layout(DecodeArgs* a, const SmemDims& d)
     take(&a->sm_code, (int)sizeof(DevCode));
     take(&a->sm_misc, 16);
     // message rows staged for the next step: two sets x threads x row words
-    const int rw = (d.cmax + 2 + 15) / 16;
-    take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * lane_threads(d.lanes) * rw * 16 : 0);
+    // (one 16-byte slot per thread and set: staged rows are 16 bytes)
+    take(&a->sm_msgbuf, stage_rows_in_smem(d.cmax, d.lanes) ? 2 * d.lanes * lane_threads(d.lanes) * 16 : 0);
     a->sm_total = off;
 }
 

@@ -142,8 +142,10 @@ __device__ __forceinline__ int row_byte_w(const uint32_t (&row)[W], int e)
 template <int W>
 __device__ __forceinline__ void load_row_w(uint32_t (&dst)[W], const uint32_t* src, bool pred)
 {
-    if constexpr (W == 1) {
-        dst[0] = pred ? __ldcg(src) : 0u;
+    if constexpr (W == 1 || W == 3) {
+#pragma unroll
+        for (int k = 0; k < W; k++)
+            dst[k] = pred ? __ldcg(src + k) : 0u;
     } else if constexpr (W == 2) {
         const uint2 v = pred ? __ldcg(reinterpret_cast<const uint2*>(src)) : make_uint2(0, 0);
         dst[0] = v.x;
@@ -163,8 +165,10 @@ __device__ __forceinline__ void load_row_w(uint32_t (&dst)[W], const uint32_t* s
 template <int W>
 __device__ __forceinline__ void store_row_w(uint32_t* dst, const uint32_t (&v)[W])
 {
-    if constexpr (W == 1) {
-        __stcg(dst, v[0]);
+    if constexpr (W == 1 || W == 3) {
+#pragma unroll
+        for (int k = 0; k < W; k++)
+            __stcg(dst + k, v[k]);
     } else if constexpr (W == 2) {
         __stcg(reinterpret_cast<uint2*>(dst), make_uint2(v[0], v[1]));
     } else {
@@ -598,7 +602,7 @@ __device__ void decode_frame(const DecodeArgs& a, const DevCode& c, unsigned cha
                              const SmemCode& t, const Job& job)
 {
     constexpr bool SAT = MODE == 0;
-    constexpr int W = row_words(CMAX);
+    constexpr int W = row_words(CMAX, LANES);
     const int tid = threadIdx.x;
     constexpr int LT = lane_threads(LANES);
     const int lane = (LANES == 2 && tid >= LT) ? 1 : 0;
