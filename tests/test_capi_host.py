@@ -141,3 +141,23 @@ def test_constellation_known_answers(built_lib):
         c = cs.modcod_info(E.MOD_32APSK, r, 0)["points"].astype(np.complex128)
         r1, r2, r3 = abs(c[17]), abs(c[0]), abs(c[8])
         assert abs(r2 / r1 - g1) < 1e-6 * g1 * 10 and abs(r3 / r1 - g2) < 1e-6 * g2 * 10
+
+
+def test_slot_buckets_waste_at_most_one_half(built_lib):
+    """Every code's kernel class (circulant-slot bucket) holds its largest
+    layer, and its check rows of cmax + 2 slots take as many packed edge
+    pairs as the real edges need: at most one half of a pair is an absent
+    slot or the pad."""
+    import cusat_gb300 as cs
+    from cusat_gb300 import enums as E
+    n = 0
+    for fs in (E.FECFRAME_NORMAL, E.FECFRAME_SHORT, E.FECFRAME_MEDIUM):
+        for r in range(E.RATE_COUNT):
+            try:
+                ci = cs.code_info(fs, r)
+            except Exception:
+                continue
+            n += 1
+            assert ci["cmax"] >= ci["cnt_max"], (fs, r)
+            assert (ci["cmax"] + 3) // 2 == (ci["cnt_max"] + 3) // 2, (fs, r, ci["cmax"], ci["cnt_max"])
+    assert n >= 56
