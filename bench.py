@@ -117,6 +117,14 @@ def n_bufs_for(wl, gen):
     return max(N_BUFS, int(np.ceil(L2_BYTES / batch_bytes)))
 
 
+def frames_per_cta_for(ci, pipe, B, sms):
+    """Frames per CTA for `pipe` chains of B-frame batches: the library's
+    default looks at one launch; with the chains' batches in flight the
+    short codes of at most 5 slots take frame pairs once the frames in
+    flight give every SM two."""
+    return 2 if ci["cmax"] <= 5 and pipe * B >= 2 * sms else 0
+
+
 def single_config(wl, nb, batch_bytes):
     """The workload's config dict, the same in both arms (nothing measured)."""
     return {"workload": f"{wl['name']} ({wl['code']}), {wl['frames']} frames, Es/N0 {wl['esn0_db']} dB: demap + "
@@ -351,11 +359,8 @@ def main():
     h_out = [(torch.zeros((B, k_bytes), dtype=torch.uint8).pin_memory(),
               torch.zeros(B, dtype=torch.int32).pin_memory(),
               torch.zeros(B, dtype=torch.int32).pin_memory()) for _ in range(pipe)]
-    # frames per CTA: the library's default looks at one launch; with
-    # `pipe` batches in flight the short 3- and 5-slot codes take frame
-    # pairs once the frames in flight give every SM two
     sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
-    fpc = 2 if ci["cmax"] <= 5 and pipe * B >= 2 * sms else 0
+    fpc = frames_per_cta_for(ci, pipe, B, sms)
     for o in rxs + decs:
         o.set_frames_per_cta(fpc)
     fpc_used = decs[0].frames_per_cta(B)

@@ -61,6 +61,11 @@ def test_bench_batches_match_oracle(cuda, which):
     B, T = wl["frames"], wl["max_trials"]
     mod, rate, fs = wl["mod"], wl["rate"], wl["fs"]
     rx = cs.rx_fec(mod, rate, fs, T, B)
+    # frames per CTA as the bench chooses them (frame pairs for the short
+    # workload's eight chains)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    pipe = min(8, max(bench.PIPE, -(-bench.RESIDENT_CTAS // B)))
+    rx.set_frames_per_cta(bench.frames_per_cta_for(cs.code_info(fs, rate), pipe, B, sms))
     dm = cs.demapper_cuda(mod, rate, fs, B)
     st = torch.cuda.current_stream()
     hard = torch.zeros((B, ci["k_ldpc"] // 8), dtype=torch.uint8, device="cuda")
