@@ -151,28 +151,77 @@ __device__ __forceinline__ void demap_logmap(const DevDemap& d, const float2* pt
         s0[b] = 0.0f;
         s1[b] = 0.0f;
     }
-#pragma unroll (logmap_unroll(NM))
-    for (int i = 0; i < np; i++) {
-        const float2 p = pts[i];
-        const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
-        const float dd = __fmaf_rn(dr, dr, __fmul_rn(di, di));
+    if constexpr (NM >= 5) {
+        // groups of 16 points: the 4 low label bits are known at compile
+        // time (one min each), the high bits are constant over a group (one
+        // min of the group's minimum each).  The same minima as point by
+        // point.
+#pragma unroll 1
+        for (int h = 0; h < (1 << (NM - 4)); h++) {
+            float mg = 1e30f;
 #pragma unroll
-        for (int b = 0; b < MB; b++) {
-            if (NM || b < nm) {
-                if (i & (1 << (nm - 1 - b))) {
-                    if (dd < mn1[b]) mn1[b] = dd;
-                } else {
-                    if (dd < mn0[b]) mn0[b] = dd;
+            for (int u = 0; u < 16; u++) {
+                const float2 p = pts[(h << 4) | u];
+                const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
+                const float dd = __fmaf_rn(dr, dr, __fmul_rn(di, di));
+#pragma unroll
+                for (int b = NM - 4; b < NM; b++) {
+                    if (u & (1 << (NM - 1 - b)))
+                        mn1[b] = fminf(mn1[b], dd);
+                    else
+                        mn0[b] = fminf(mn0[b], dd);
+                }
+                mg = fminf(mg, dd);
+            }
+#pragma unroll
+            for (int b = 0; b < NM - 4; b++) {
+                if (h & (1 << (NM - 5 - b)))
+                    mn1[b] = fminf(mn1[b], mg);
+                else
+                    mn0[b] = fminf(mn0[b], mg);
+            }
+        }
+    } else {
+#pragma unroll (logmap_unroll(NM))
+        for (int i = 0; i < np; i++) {
+            const float2 p = pts[i];
+            const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
+            const float dd = __fmaf_rn(dr, dr, __fmul_rn(di, di));
+#pragma unroll
+            for (int b = 0; b < MB; b++) {
+                if (NM || b < nm) {
+                    if (i & (1 << (nm - 1 - b))) {
+                        if (dd < mn1[b]) mn1[b] = dd;
+                    } else {
+                        if (dd < mn0[b]) mn0[b] = dd;
+                    }
                 }
             }
         }
     }
     const float scale = __fmul_rn(llr_gain, 0.25f);
+    // A point whose (dd - M) * scale is at least 16, M the largest of the
+    // per-bit minima, has every per-bit delta (dd - mn) * scale >= 16 --
+    // subtraction and multiplication by a positive scale are monotone under
+    // round-to-nearest and mn <= M -- so none of its terms enters a sum:
+    // it is skipped with one test instead of one per bit (same sums).
+    // From 32 points up (measured: 256APSK 3.35 -> 2.79 ms per 256 normal
+    // frames; 16 points and fewer were faster without the test).
+    float M = 0.0f;
+#pragma unroll
+    for (int b = 0; b < MB; b++)
+        if (NM || b < nm)
+            M = fmaxf(M, fmaxf(mn0[b], mn1[b]));
 #pragma unroll (logmap_unroll(NM))
     for (int i = 0; i < np; i++) {
         const float2 p = pts[i];
         const float dr = __fsub_rn(re, p.x), di = __fsub_rn(im, p.y);
         const float dd = __fmaf_rn(dr, dr, __fmul_rn(di, di));
+        if (NM == 0 || NM >= 5) {
+            const bool near = valid && __fmul_rn(__fsub_rn(dd, M), scale) < 16.0f;
+            if (VOTE ? !__any_sync(0xffffffffu, near) : !near)
+                continue;
+        }
 #pragma unroll
         for (int b = 0; b < MB; b++) {
             if (NM || b < nm) {
