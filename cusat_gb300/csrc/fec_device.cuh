@@ -122,9 +122,11 @@ __device__ __forceinline__ void demap_8psk(const DevDemap& d, float re, float im
 // its bits' exps inline, and past a few KB of loop body the warps wait on
 // instruction fetch (ncu, 256APSK unrolled by 16: 9.9 of 15.9 cycles per
 // issue stalled on no instruction).  Measured best on GB300 (demap of 256
-// normal frames): 16 points for up to 16 points, 8 for 32 and 64, 4 for 128
-// and 256 (256APSK 4.25 -> 2.73 ms, 128APSK 2.08 -> 1.41 ms).
-__host__ __device__ constexpr int logmap_unroll(int nm) { return nm == 0 ? 1 : nm <= 4 ? 16 : nm <= 6 ? 8 : 4; }
+// normal frames): 16 points for up to 16 points, 8 for 32, 4 for 64 to 256
+// (256APSK 4.25 -> 2.73 ms, 128APSK 2.08 -> 1.41 ms; with the grouped first
+// pass and the point skip, 2 and 8 lose at 128-256 points and 4 gains 1 %
+// at 64).
+__host__ __device__ constexpr int logmap_unroll(int nm) { return nm == 0 ? 1 : nm <= 4 ? 16 : nm <= 5 ? 8 : 4; }
 
 // APSK: log-MAP over the points (pts in shared memory), NM bits per symbol
 // (0: d.n_mod at run time; a compile-time NM resolves every label-bit test
