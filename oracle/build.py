@@ -82,7 +82,69 @@ def build_ref(verbose=False):
     return out
 
 
+REF_KERNELS = {
+    "ref_ldpc_decode.sm_103.cubin": "lib/cusat_dsp/cuda/ldpc_decode_kernel.cu",
+    "ref_demap.sm_103.cubin": "lib/cusat_dsp/cuda/demapper_kernel.cu",
+}
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def ref_cubin_paths():
+    return {k: os.path.join(HERE, "_ref", k) for k in REF_KERNELS}
+
+
+def build_ref_cubins(verbose=False):
+    """Compile the reference's decoder and demapper kernels into cubins;
+    returns the paths, or None when the reference tree or nvcc is absent."""
+    nvcc = os.path.join(CUDA_HOME, "bin", "nvcc")
+    if not os.path.isdir(os.path.join(REF, "lib", "cusat_dsp")) or not os.path.exists(nvcc):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    inc = ["-I" + os.path.join(REF, "lib", "cusat_dsp", "include"), "-I" + os.path.join(REF, "lib", "cusat_dsp")]
+    outs = ref_cubin_paths()
+    for name, src in REF_KERNELS.items():
+        out, src = outs[name], os.path.join(REF, src)
+        if _newer(out, [src]):
+            continue
+        # CMake Release flags of the reference (-O3 -DNDEBUG, C++17) for
+        # CMAKE_CUDA_ARCHITECTURES=103
+        cmd = [nvcc, "-O3", "-DNDEBUG", "-std=c++17", "-gencode", "arch=compute_103,code=sm_103", "-cubin",
+               *inc, "-o", out + ".tmp", src]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.check_call(cmd)
+        os.replace(out + ".tmp", out)
+    return outs
+
+
+def build_ref_gpu(verbose=False):
+    """Compile ref_gpu.c (driver-API launcher of the reference cubins);
+    returns the path, or None without the CUDA headers."""
+    cuda_h = os.path.join(CUDA_HOME, "include", "cuda.h")
+    if not os.path.exists(cuda_h):
+        return None
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libref_gpu.so")
+    src = os.path.join(HERE, "ref_gpu.c")
+    deps = [src, os.path.join(HERE, "..", "cusat_gb300", "csrc", "cusat_data.h"),
+            os.path.join(HERE, "..", "cusat_gb300", "csrc", "gen", "code_tables.inc")]
+    if _newer(out, deps):
+        return out
+    libdirs = [os.path.join(CUDA_HOME, "lib64", "stubs"), os.path.join(CUDA_HOME, "lib64")]
+    cmd = ["gcc", "-std=c99", "-O2", "-fPIC", "-shared", "-I" + os.path.join(CUDA_HOME, "include"),
+           "-o", out + ".tmp", src, *["-L" + d for d in libdirs], "-lcuda"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(verbose=True))
     print(build_ref(verbose=True))
+    print(build_ref_cubins(verbose=True))
+    print(build_ref_gpu(verbose=True))
     sys.exit(0)

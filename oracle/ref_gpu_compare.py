@@ -1,0 +1,221 @@
+"""The reference's own GPU kernels beside this project's, on one GPU.
+
+TEST INFRASTRUCTURE: runs the reference's demapper and layered decoder
+(compiled unchanged into oracle/_ref/*.cubin by oracle/build.py, launched
+by oracle/ref_gpu.c) on the same inputs as this project's kernels and the
+oracle, and prints one JSON object:
+
+  demap    per MODCOD: the reference kernel's int16 LLRs against the
+           oracle's (count equal, largest difference)
+  decode   per workload: the reference decoder's (hard bits, trials) per
+           frame against the oracle's (identical, same hard bits, both
+           converged), and against a second run of itself
+  timing   per workload: CUDA-event time per launch of the reference
+           decoder and of this project's decoder on the same LLR batches,
+           one launch after another on one stream, inputs cycled over
+           batches larger than the L2 together; the same for the demappers
+
+Usage (on a GPU host, after __graft_entry__.build()):
+    python oracle/ref_gpu_compare.py [--out FILE] [--steps K] [--warmup W]
+"""
+import argparse
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+# (name, MODCOD, frame size, frames, Es/N0 dB, seed)
+DECODE_CASES = [
+    ("C2 normal 3/5 8PSK", "8psk3/5", 0, 256, 6.0, 2024),
+    ("C1 short 1/2 QPSK", "qpsk1/2", 1, 64, 1.5, 2025),
+    ("normal 1/4 QPSK", "qpsk1/4", 0, 256, None, 31),
+    ("normal 9/10 8PSK", "8psk9/10", 0, 256, None, 32),
+    ("short 5/6 16APSK", "16apsk5/6", 1, 256, None, 33),
+]
+DEMAP_CASES = [("qpsk1/2", 1), ("qpsk3/4", 0), ("8psk3/5", 0), ("8psk8/9", 1), ("8apsk5/9", 0),
+               ("16apsk2/3", 0), ("16apsk5/6", 1), ("32apsk3/4", 0), ("64apsk32/45", 0), ("128apsk3/4", 0),
+               ("256apsk3/4", 0), ("256apsk32/45", 0)]
+L2_BYTES = 160e6
+
+
+def traffic(cs, E, O, name, fs, B, esn0, seed, n_bufs=1):
+    """Noisy symbols (the bench's recipe: one set of codewords, fresh noise
+    per buffer), N0, the capped gain and the MODCOD description."""
+    _, mod, rate, _, _, thr = E.find_modcod(name)
+    esn0 = thr + 0.5 if esn0 is None else esn0
+    rng = np.random.default_rng(seed)
+    ci = cs.code_info(fs, rate)
+    msg = rng.integers(0, 256, (B, ci["k_bch"] // 8), dtype=np.uint8)
+    sym = cs.map_frames(mod, rate, fs, cs.encode_frames(fs, rate, msg))
+    es = float(np.mean(sym.astype(np.float64) ** 2) * 2)
+    sym = (sym / np.float32(np.sqrt(es))).astype(np.float32)
+    n0 = np.float32(1.0 / 10 ** (esn0 / 10.0))
+    sigma = np.float32(np.sqrt(n0 / np.float32(2.0)))
+    bufs = [(sym + sigma * rng.standard_normal(sym.shape, dtype=np.float32)).astype(np.float32)
+            for _ in range(n_bufs)]
+    mi = O.modcod(mod, rate, fs)
+    gain = O.capped_llr_gain(mi, min(4.0 / float(n0), 1000.0))
+    return mod, rate, esn0, bufs, float(n0), gain, mi
+
+
+def time_launches(torch, launch, n_inputs, steps, warmup):
+    """ms per launch: warmup untimed launches, then steps launches timed
+    with CUDA events on the current stream, inputs cycled."""
+    s = torch.cuda.current_stream()
+    for i in range(warmup):
+        launch(i % n_inputs)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for i in range(steps):
+        launch(i % n_inputs)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def demap_section(torch, cs, E, O, rg):
+    out = []
+    s = torch.cuda.current_stream()
+    for name, fs in DEMAP_CASES:
+        mod, rate, esn0, bufs, n0, gain, mi = traffic(cs, E, O, name, fs, 8, None, 41)
+        sym = bufs[0]
+        ref = O.demap_modcod(sym, mi, n0, gain)
+        pts = mi["points"]
+        d_re = torch.from_numpy(np.ascontiguousarray(pts.real, np.float32)).cuda()
+        d_im = torch.from_numpy(np.ascontiguousarray(pts.imag, np.float32)).cuda()
+        d_sym = torch.from_numpy(sym).cuda()
+        d_out = torch.zeros((8, mi["fecframe_len"]), dtype=torch.int16, device="cuda")
+        rg.demap(d_sym, d_out, d_re, d_im, mi, n0, gain, 8, s)
+        torch.cuda.synchronize()
+        got = d_out.cpu().numpy().astype(np.int32)
+        diff = np.abs(got - ref.astype(np.int32))
+        out.append({"modcod": name, "fs": fs, "esn0_db": round(esn0, 2), "llrs": int(diff.size),
+                    "equal": int((diff == 0).sum()), "max_abs_diff": int(diff.max()),
+                    "diff_hist": {str(int(k)): int(v) for k, v in zip(*np.unique(diff, return_counts=True))}})
+    return out
+
+
+def decode_section(torch, cs, E, O, rg, steps, warmup):
+    out = []
+    s = torch.cuda.current_stream()
+    for label, name, fs, B, esn0, seed in DECODE_CASES:
+        _, mod, rate, _, _, _ = E.find_modcod(name)
+        mi0 = O.modcod(mod, rate, fs)
+        batch_bytes = B * mi0["fecframe_len"] * 2
+        nb = max(4, int(np.ceil(L2_BYTES / batch_bytes)))
+        mod, rate, esn0, bufs, n0, gain, mi = traffic(cs, E, O, name, fs, B, esn0, seed, nb)
+        llr0 = O.demap_modcod(bufs[0], mi, n0, gain)
+        ho, to = O.ldpc_decode(fs, rate, llr0, 50, nthreads=os.cpu_count() or 8)
+        # LLR batches on the device (this project's demapper, bit-exact with
+        # the oracle's; checked on the first batch)
+        dm = cs.demapper_cuda(mod, rate, fs, B)
+        llrs = []
+        for b in bufs:
+            d = torch.zeros((B, mi["fecframe_len"]), dtype=torch.int16, device="cuda")
+            dm.demap_launch(torch.from_numpy(b).cuda(), B, n0, gain, d, s)
+            llrs.append(d)
+        torch.cuda.synchronize()
+        assert (llrs[0].cpu().numpy() == llr0).all(), "device LLRs differ from the oracle's"
+        kb = O.code_info(fs, rate)["K"] // 8
+        rdec = rg.decoder(fs, rate, 50, B)
+        ours = cs.ldpc_decode_cuda(fs, rate, 50, B)
+        rh = torch.zeros((B, kb), dtype=torch.uint8, device="cuda")
+        rt = torch.zeros(B, dtype=torch.int32, device="cuda")
+        oh = torch.zeros((B, kb), dtype=torch.uint8, device="cuda")
+        ot = torch.zeros(B, dtype=torch.int32, device="cuda")
+        runs = []
+        for _ in range(2):
+            rdec.launch(llrs[0], B, rh, rt, s)
+            torch.cuda.synchronize()
+            runs.append((rh.cpu().numpy().copy(), rt.cpu().numpy().copy()))
+        ours.decode_launch_async(llrs[0], B, s, oh, ot)
+        torch.cuda.synchronize()
+        hg, tg = oh.cpu().numpy(), ot.cpu().numpy()
+        (h1, t1), (h2, t2) = runs
+        same_hard = ~(h1 != ho).any(axis=1)
+        conv = (t1 >= 0) & (to >= 0)
+        rec = {"workload": label, "modcod": name, "fs": fs, "frames": B, "esn0_db": round(esn0, 2),
+               "ref_schedule_steps": rdec.n_steps,
+               "oracle_failed": int((to < 0).sum()), "ref_failed": int((t1 < 0).sum()),
+               "oracle_mean_iterations": float(np.mean(np.where(to >= 0, 50 - to, 50))),
+               "ref_mean_iterations": float(np.mean(np.where(t1 >= 0, 50 - t1, 50))),
+               "ref_vs_oracle_identical": int((same_hard & (t1 == to)).sum()),
+               "ref_vs_oracle_same_hard": int(same_hard.sum()),
+               "both_converged": int(conv.sum()),
+               "both_converged_same_hard": int((conv & same_hard).sum()),
+               "ref_run_to_run_identical": int((~(h1 != h2).any(axis=1) & (t1 == t2)).sum()),
+               "ours_vs_oracle_identical": int((~(hg != ho).any(axis=1) & (tg == to)).sum())}
+        # timing: the same LLR batches, one launch after another on one stream
+        k_info = O.code_info(fs, rate)["K"]
+        ms_ref = time_launches(torch, lambda i: rdec.launch(llrs[i], B, rh, rt, s), nb, steps, warmup)
+        ms_ours = time_launches(torch, lambda i: ours.decode_launch_async(llrs[i], B, s, oh, ot), nb, steps,
+                                warmup)
+        rec["timing"] = {"batches_cycled": nb, "steps": steps, "warmup": warmup,
+                         "ref_ms_per_launch": ms_ref, "ours_ms_per_launch": ms_ours,
+                         "ref_info_gbps": B * k_info / (ms_ref * 1e6),
+                         "ours_info_gbps": B * k_info / (ms_ours * 1e6),
+                         "speedup": ms_ref / ms_ours}
+        rdec.close()
+        ours.close()
+        out.append(rec)
+        print(json.dumps(rec), file=sys.stderr)
+    return out
+
+
+def demap_timing(torch, cs, E, O, rg, steps, warmup):
+    """Both demappers on the headline batch (256 normal 8PSK 3/5 frames)."""
+    s = torch.cuda.current_stream()
+    out = []
+    for name, fs, B in [("8psk3/5", 0, 256), ("32apsk3/4", 0, 256), ("256apsk32/45", 0, 256)]:
+        mod, rate, esn0, _, n0, gain, mi = traffic(cs, E, O, name, fs, B, None, 51)
+        sym_bytes = B * mi["xfecframe_len"] * 8
+        nb = max(4, int(np.ceil(L2_BYTES / sym_bytes)))
+        _, _, _, bufs, _, _, _ = traffic(cs, E, O, name, fs, B, None, 51, nb)
+        d_syms = [torch.from_numpy(b).cuda() for b in bufs]
+        pts = mi["points"]
+        d_re = torch.from_numpy(np.ascontiguousarray(pts.real, np.float32)).cuda()
+        d_im = torch.from_numpy(np.ascontiguousarray(pts.imag, np.float32)).cuda()
+        d_out = torch.zeros((B, mi["fecframe_len"]), dtype=torch.int16, device="cuda")
+        dm = cs.demapper_cuda(mod, rate, fs, B)
+        ms_ref = time_launches(torch, lambda i: rg.demap(d_syms[i], d_out, d_re, d_im, mi, n0, gain, B, s), nb,
+                               steps, warmup)
+        ms_ours = time_launches(torch, lambda i: dm.demap_launch(d_syms[i], B, n0, gain, d_out, s), nb, steps,
+                                warmup)
+        out.append({"modcod": name, "fs": fs, "frames": B, "batches_cycled": nb, "ref_ms_per_launch": ms_ref,
+                    "ours_ms_per_launch": ms_ours, "speedup": ms_ref / ms_ours})
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default="")
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    args = ap.parse_args()
+    import torch
+
+    import cusat_gb300 as cs
+    import oracle_lib as O
+    from cusat_gb300 import enums as E
+
+    torch.cuda.set_device(0)
+    rg = O.RefGpu()
+    res = {"gpu": torch.cuda.get_device_name(0), "demap": demap_section(torch, cs, E, O, rg)}
+    print(json.dumps(res["demap"]), file=sys.stderr)
+    res["decode"] = decode_section(torch, cs, E, O, rg, args.steps, args.warmup)
+    res["demap_timing"] = demap_timing(torch, cs, E, O, rg, args.steps, args.warmup)
+    line = json.dumps(res)
+    print(line)
+    if args.out:
+        with open(args.out, "w") as f:
+            f.write(line + "\n")
+
+
+if __name__ == "__main__":
+    main()

@@ -305,3 +305,80 @@ def pl_frame_payload(data, slots, pilots, r):
     out[:, 0] = np.select([rr == 0, rr == 1, rr == 2, rr == 3], [re, -im, -re, im])
     out[:, 1] = np.select([rr == 0, rr == 1, rr == 2, rr == 3], [im, re, -im, -re])
     return out.reshape(-1)
+
+
+class RefGpu:
+    """The reference's own demapper and layered-decoder kernels, compiled
+    unchanged into oracle/_ref/*.cubin and launched through oracle/ref_gpu.c
+    the way the reference's host classes launch them
+    (demapper_kernel.cu:293-330, ldpc_decode_kernel.cu:991-1285).  Test
+    infrastructure: it holds the reference's kernels against the oracle and
+    times them beside this project's kernels on the same GPU."""
+
+    def __init__(self):
+        import sys
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import build as _b
+        sys.path.pop(0)
+        paths = _b.ref_cubin_paths()
+        missing = [p for p in paths.values() if not os.path.exists(p)]
+        if missing:
+            raise FileNotFoundError(f"reference cubins not built: {missing}")
+        so = _b.build_ref_gpu()
+        if so is None:
+            raise FileNotFoundError("cuda.h not found: oracle/ref_gpu.c not built")
+        L = ctypes.CDLL(so)
+        L.rg_last_error.restype = ctypes.c_char_p
+        L.rg_dec_create.restype = ctypes.c_void_p
+        L.rg_dec_create.argtypes = [ctypes.c_int] * 4
+        L.rg_dec_destroy.argtypes = [ctypes.c_void_p]
+        L.rg_dec_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.rg_dec_launch.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64,
+                                    ctypes.c_uint64, ctypes.c_void_p]
+        L.rg_demap_launch.argtypes = [ctypes.c_uint64] * 4 + [ctypes.c_int] * 5 + [
+            ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]
+        self.L = L
+        self._check(L.rg_open(paths["ref_ldpc_decode.sm_103.cubin"].encode(),
+                              paths["ref_demap.sm_103.cubin"].encode()))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.L.rg_last_error().decode())
+
+    def decoder(self, fs, rate, max_trials, max_batch):
+        return RefGpuDecoder(self, fs, rate, max_trials, max_batch)
+
+    def demap(self, sym_dev, out_dev, pts_re_dev, pts_im_dev, mi, noise_var, llr_gain, B, stream):
+        """demap_deinterleave_kernel of B frames; llr_gain already capped.
+        QPSK and 8PSK get no point table, as demapper_cuda uploads one only
+        for 8APSK and the 16+ point families (demapper_kernel.cu:252-262):
+        its 8PSK formula branch is taken only without a table (:76)."""
+        col = np.ascontiguousarray(mi["col_offset"], np.uint32)
+        table = mi["kind"] == 2
+        re_p = pts_re_dev.data_ptr() if table else 0
+        im_p = pts_im_dev.data_ptr() if table else 0
+        self._check(self.L.rg_demap_launch(sym_dev.data_ptr(), out_dev.data_ptr(), re_p,
+                                           im_p, mi["xfecframe_len"], mi["interleaved_len"],
+                                           mi["fecframe_len"], mi["n_mod"], mi["n_points"], col.ctypes.data,
+                                           noise_var, llr_gain, B, stream.cuda_stream))
+
+
+class RefGpuDecoder:
+    def __init__(self, rg, fs, rate, max_trials, max_batch):
+        self.rg = rg
+        h = rg.L.rg_dec_create(fs, rate, max_trials, max_batch)
+        if not h:
+            raise RuntimeError(rg.L.rg_last_error().decode())
+        self.h = h
+        info = np.zeros(8, np.int32)
+        rg.L.rg_dec_info(h, info.ctypes.data)
+        self.N, self.K, self.R, self.q, self.cnl, self.lt_alloc, self.n_steps, self.smem = (int(v) for v in info)
+
+    def launch(self, llr_dev, B, hard_dev, result_dev, stream):
+        self.rg._check(self.rg.L.rg_dec_launch(self.h, llr_dev.data_ptr(), B, hard_dev.data_ptr(),
+                                               result_dev.data_ptr(), stream.cuda_stream))
+
+    def close(self):
+        if self.h:
+            self.rg.L.rg_dec_destroy(self.h)
+            self.h = None
