@@ -156,6 +156,8 @@ def parse():
                     help="codes: comma-separated MODCOD names for the demapper table (default: one per family)")
     ap.add_argument("--learned", action="store_true",
                     help="mixed/serve: decode each MODCOD with its adopted learned weights where one exists")
+    ap.add_argument("--no-extra", dest="extra", action="store_false",
+                    help="single, N=1: skip the other configurations' runs summarised under \"workloads\"")
     return ap.parse_args()
 
 
@@ -289,6 +291,51 @@ def reference_arm(args, wl):
                                        f"(the reference ships no CPU decoder: C restatement of its algorithm)"},
             "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# The other configurations, run after the headline's timed region as
+# separate processes of this script (each with its own warm-up, CUDA-event
+# timing and clock record) and summarised in the headline line, so that one
+# default run records every configuration.
+EXTRA_WORKLOADS = [
+    ("C1", ["--workload", "short"]),
+    ("C3", ["--workload", "mixed"]),
+    ("C4", ["--workload", "learned"]),
+    ("C5", ["--workload", "serve", "--rates", "3,4", "--duration", "0.25"]),
+]
+
+
+def extra_workloads(args):
+    out = {}
+    for key, extra in EXTRA_WORKLOADS:
+        cmd = [sys.executable, os.path.abspath(__file__), "--steps", str(args.steps), "--warmup", str(args.warmup),
+               "--cpu-seconds", "3", *extra]
+        t0 = time.time()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+            line = json.loads([x for x in r.stdout.splitlines() if x.startswith("{")][-1])
+        except Exception as e:  # a failed extra run is recorded, not fatal to the headline
+            out[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
+            continue
+        summ = {"cmd": "python bench.py " + " ".join(cmd[2:]), "workload": line["config"].get("workload"),
+                "value": line.get("value"), "unit": line.get("unit"), "ms_per_step": line.get("ms_per_step"),
+                "wall_s": round(time.time() - t0, 1)}
+        for k in ("e2e", "cpu_baseline", "clocks", "gpu_launches"):
+            if k in line:
+                summ[k] = {kk: vv for kk, vv in line[k].items() if kk != "path"} if isinstance(line[k], dict) \
+                    else line[k]
+        st = line.get("stats", {})
+        for k in ("batch_latency_ms", "mean_iterations", "frames_failed", "frames_per_cta"):
+            if k in st:
+                summ[k] = st[k]
+        cfg = line["config"]
+        if key == "C4":
+            summ.update({k: cfg[k] for k in ("learned", "plain", "speedup")})
+        if key == "C5":
+            summ.update({"rates": [{k: r_.get(k) for k in ("rate_gsym_s", "offered_gsym_s", "info_gbit_s", "p50_ms", "p99_ms", "failed")
+                                    if k in r_} for r_ in cfg["rates"]]})
+        out[key] = summ
+    return out
 
 
 def load_peaks():
@@ -532,6 +579,8 @@ def main():
         "gpu_launches": 3 * args.steps,  # demap, decoder, BCH check per step
         "wall_s": wall,
     }
+    if args.workload == "single" and world == 1 and args.extra:
+        line["workloads"] = extra_workloads(args)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
