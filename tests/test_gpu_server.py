@@ -1,6 +1,7 @@
 """Serving loop: every frame's hard decisions, iteration count and BCH flag
 are identical whether it is decoded alone (a one-frame rx_fec launch) or
-admitted into mixed batches next to other requests; the HBM budget bounds
+admitted into mixed batches next to other requests, and equal to the
+oracle's demap -> decode -> BCH check of that frame; the HBM budget bounds
 the in-flight bytes; per-MODCOD learned weights apply."""
 import ctypes
 
@@ -8,6 +9,7 @@ import numpy as np
 import pytest
 
 import cusat_gb300 as cs
+import oracle_lib as O
 from cusat_gb300 import enums as E
 from cusat_gb300 import serving
 
@@ -32,6 +34,17 @@ def alone(torch, pool, e, f, T, weights=None):
     rx.launch(ent["sym"][f:f + 1], 1, ent["n0"], ent["gain"], h, t, v, torch.cuda.current_stream())
     torch.cuda.synchronize()
     return h.cpu().numpy()[0], int(t.item()), int(v.item())
+
+
+def oracle(pool, e, f, T):
+    """The oracle's chain on frame f of entry e (its own demap parameters)."""
+    mod, rate, fs = pool.modcods[e]
+    ent = pool.entries[e]
+    sym = ent["sym"][f:f + 1].cpu().numpy()
+    llr = O.demap_modcod(sym, O.modcod(mod, rate, fs), ent["n0"], ent["gain"])
+    hard, trials = O.ldpc_decode(fs, rate, llr, T)
+    _, valid = O.bch_check(fs, rate, hard)
+    return hard[0], int(trials[0]), int(valid[0] != 0)
 
 
 def run(srv, pool, trace, lead_s=0.02):
@@ -77,6 +90,10 @@ def test_results_identical_alone_and_in_mix(cuda, pool):
             ref[(e, f)] = alone(torch, pool, e, f, T)
         hr, tr, vr = ref[(e, f)]
         assert (r.trials, r.bch_valid) == (tr, vr) and (h == hr).all()
+    # and each distinct frame as the oracle decodes it
+    for (e, f), (hr, tr, vr) in ref.items():
+        ho, to, vo = oracle(pool, e, f, T)
+        assert (tr, int(vr != 0)) == (to, vo) and (hr == ho).all(), f"entry {e} frame {f} differs from the oracle"
     srv.close()
 
 
