@@ -190,7 +190,6 @@ rg_dec* rg_dec_create(int framesize, int rate, int max_trials, int max_batch)
     TRY(cuMemAlloc(&d->data, (size_t)max_batch * d->K * 2));
     TRY(cuMemAlloc(&d->pty, (size_t)max_batch * R * 2));
     TRY(cuMemAlloc(&d->bnl, (size_t)max_batch * d->lt_alloc));
-    TRY(cuFuncSetAttribute(g_dec_fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)d->smem));
 #undef TRY
     free(pos_raw);
     free(cnc_raw);
@@ -225,6 +224,9 @@ int rg_dec_launch(rg_dec* d, CUdeviceptr llr, int B, CUdeviceptr hard, CUdevicep
     int N = d->N, syn = 1, steps = d->n_steps;
     void* args[] = {&d->data, &d->pty, &d->bnl, &d->pos, &d->cnc, &d->layer_off, &result, &hard,
                     &K, &R, &M, &q, &CNL, &LT, &T, &llr, &N, &syn, &d->sched, &steps};
+    /* this code's shared-memory opt-in (decoders of other codes may have set another) */
+    CU(cuFuncSetAttribute(g_dec_fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)d->smem),
+       "decoder shared-memory opt-in");
     CU(cuLaunchKernel(g_dec_fn, (unsigned)B, 1, 1, 2 * RG_M, 1, 1, d->smem, s, args, 0), "decoder launch");
     return 0;
 }
