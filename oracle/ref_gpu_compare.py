@@ -17,9 +17,11 @@ oracle, and prints one JSON object:
   mixed    the bench's 1024-frame mixed batch: this project's graph replay
            against the reference's demap + decoder per MODCOD entry on
            concurrent streams, one round at a time
+  fer      frame error rates of both decoders on the same fresh GPU-made
+           LLRs near the waterfall of C1's and C2's codes
 
 Usage (on a GPU host, after __graft_entry__.build()):
-    python oracle/ref_gpu_compare.py [--out FILE] [--steps K] [--warmup W]
+    python oracle/ref_gpu_compare.py [--out FILE] [--steps K] [--warmup W] [--no-fer]
 """
 import argparse
 import json
@@ -279,11 +281,61 @@ def mixed_section(torch, cs, O, rg, steps, warmup):
                     "decoder per MODCOD entry on concurrent streams (no BCH)"}
 
 
+# (MODCOD, frame size, Es/N0 dB, frames): near the waterfall of C1's and C2's codes
+FER_POINTS = [("qpsk1/2", 1, 1.25, 51200), ("qpsk1/2", 1, 1.5, 51200), ("8psk3/5", 0, 5.5, 25600),
+              ("8psk3/5", 0, 5.6, 25600), ("8psk3/5", 0, 5.7, 25600)]
+
+
+def fer_section(torch, cs, rg, points=FER_POINTS, batch=256, seed=7):
+    """Frame error rates of the reference decoder kernel and this project's
+    decoder on the same LLRs: fresh random messages encoded, mapped and
+    demapped on the GPU by this library (learned.ChannelPool), AWGN per
+    frame, max 50 iterations; a frame error is any information bit wrong."""
+    from cusat_gb300 import learned
+    out = []
+    s = torch.cuda.current_stream()
+    for name, fs, esn0, n_frames in points:
+        pool = learned.ChannelPool(name, fs, 0, seed, batch, torch)
+        rate = pool.rate
+        kb = cs.code_info(fs, rate)["k_ldpc"] // 8
+        rdec = rg.decoder(fs, rate, 50, batch)
+        ours = cs.ldpc_decode_cuda(fs, rate, 50, batch)
+        rh = torch.zeros((batch, kb), dtype=torch.uint8, device="cuda")
+        rt = torch.zeros(batch, dtype=torch.int32, device="cuda")
+        oh = torch.zeros_like(rh)
+        ot = torch.zeros_like(rt)
+        err_ref = err_ours = fail_ref = fail_ours = it_ref = it_ours = 0
+        for _ in range(n_frames // batch):
+            _, llr, cw, _, _ = pool.draw(batch, esn0, s)
+            rdec.launch(llr, batch, rh, rt, s)
+            ours.decode_launch_async(llr, batch, s, oh, ot)
+            info = cw[:, :kb]
+            err_ref += int((rh != info).any(dim=1).sum())
+            err_ours += int((oh != info).any(dim=1).sum())
+            fail_ref += int((rt < 0).sum())
+            fail_ours += int((ot < 0).sum())
+            it_ref += int(torch.where(rt >= 0, 50 - rt, 50).sum())
+            it_ours += int(torch.where(ot >= 0, 50 - ot, 50).sum())
+        n = (n_frames // batch) * batch
+        rdec.close()
+        ours.close()
+        rec = {"modcod": name, "fs": fs, "esn0_db": esn0, "frames": n,
+               "ref_frame_errors": err_ref, "ours_frame_errors": err_ours,
+               "ref_fer": err_ref / n, "ours_fer": err_ours / n,
+               "ref_not_converged": fail_ref, "ours_not_converged": fail_ours,
+               "ref_mean_iterations": it_ref / n, "ours_mean_iterations": it_ours / n}
+        out.append(rec)
+        print(json.dumps(rec), file=sys.stderr)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default="")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--no-fer", action="store_true", help="skip the frame-error-rate comparison")
+    ap.add_argument("--fer-only", action="store_true", help="run the frame-error-rate comparison alone")
     args = ap.parse_args()
     import torch
 
@@ -293,12 +345,21 @@ def main():
 
     torch.cuda.set_device(0)
     rg = O.RefGpu()
+    if args.fer_only:
+        line = json.dumps({"gpu": torch.cuda.get_device_name(0), "fer": fer_section(torch, cs, rg)})
+        print(line)
+        if args.out:
+            with open(args.out, "w") as f:
+                f.write(line + "\n")
+        return
     res = {"gpu": torch.cuda.get_device_name(0), "demap": demap_section(torch, cs, E, O, rg)}
     print(json.dumps(res["demap"]), file=sys.stderr)
     res["decode"] = decode_section(torch, cs, E, O, rg, args.steps, args.warmup)
     res["demap_timing"] = demap_timing(torch, cs, E, O, rg, args.steps, args.warmup)
     res["mixed"] = mixed_section(torch, cs, O, rg, args.steps, args.warmup)
     print(json.dumps(res["mixed"]), file=sys.stderr)
+    if not args.no_fer:
+        res["fer"] = fer_section(torch, cs, rg)
     line = json.dumps(res)
     print(line)
     if args.out:
