@@ -7,13 +7,14 @@ are compiled unchanged into cubins where the reference tree is present
 through oracle/ref_gpu.c the way the reference's host classes launch them.
 
 - Demapper: the reference kernel's int16 LLRs equal the oracle's and this
-  project's, every LLR, for QPSK, the 8PSK formula and the log-MAP families
-  8APSK to 256APSK.
+  project's, every LLR, for every MODCOD of the ACM table and frame size
+  (QPSK, the 8PSK formula and the log-MAP families 8APSK to 256APSK).
 - Decoder: checks of one schedule step that share a bit race in the
   reference kernel (ldpc_decode_kernel.cu:793-802), so its iteration counts
   vary from run to run; the oracle resolves the race deterministically.  The
   reference's hard decisions equal the oracle's on every frame where both
-  converge, and both converge on the same frames of these workloads.
+  converge, for every code; on the benchmark workloads both converge on the
+  same frames.
 """
 import os
 
@@ -32,6 +33,30 @@ DEMAP_CASES = [("qpsk1/2", 1), ("qpsk3/4", 0), ("8psk3/5", 0), ("8psk8/9", 1), (
 # (MODCOD, frame size, frames, Es/N0 dB or None = threshold + 0.5, seed)
 DECODE_CASES = [("8psk3/5", 0, 256, 6.0, 2024), ("qpsk1/2", 1, 64, 1.5, 2025), ("8psk9/10", 0, 64, None, 32),
                 ("qpsk1/4", 0, 32, None, 31)]
+
+
+def _modcod_cases():
+    out = []
+    for m in E.MODCODS:
+        for fs in (0, 1):
+            try:
+                cs.code_info(fs, m[2])
+            except cs.CusatError:
+                continue
+            out.append((m[3], fs))
+    return out
+
+
+def _codes():
+    out = []
+    for fs in (0, 1):
+        for r in range(E.RATE_COUNT):
+            try:
+                cs.code_info(fs, r)
+            except cs.CusatError:
+                continue
+            out.append((fs, r))
+    return out
 
 
 @pytest.fixture(scope="module")
@@ -56,10 +81,11 @@ def traffic(name, fs, B, esn0, seed):
     return mod, rate, noisy.astype(np.float32), float(n0), O.capped_llr_gain(mi, min(4.0 / float(n0), 1000.0)), mi
 
 
-@pytest.mark.parametrize("name,fs", DEMAP_CASES)
+@pytest.mark.parametrize("name,fs", _modcod_cases())
 def test_reference_demapper_bit_exact(cuda, rg, name, fs):
+    # every MODCOD of the ACM table, both frame sizes where the code exists
     torch = cuda
-    B = 4
+    B = 2 if (name, fs) not in DEMAP_CASES else 4
     mod, rate, sym, n0, gain, mi = traffic(name, fs, B, None, 41)
     s = torch.cuda.current_stream()
     d_sym = torch.from_numpy(sym).cuda()
@@ -102,3 +128,41 @@ def test_reference_decoder_agrees_with_oracle(cuda, rg, name, fs, B, esn0, seed)
     assert len(bad) == 0, f"converged frames {bad[:8]} decode to different bits"
     assert conv.sum() >= B // 2  # the workload actually decodes
     print(f"{name}: trials identical on {(tr == to).sum()} of {B} frames")
+
+
+@pytest.mark.parametrize("fs,rate", _codes())
+def test_reference_decoder_every_code(cuda, rg, fs, rate):
+    # every code, noisy BPSK-like LLRs a little above its waterfall (Eb/N0
+    # rising with the rate; about 9 iterations on average, nearly every
+    # frame converging): where both converge, the reference kernel's hard
+    # bits are the oracle's
+    torch = cuda
+    ci = cs.code_info(fs, rate)
+    rng = np.random.default_rng(1000 * fs + rate)
+    B = 16
+    msg = rng.integers(0, 256, (B, ci["k_bch"] // 8), dtype=np.uint8)
+    bits = np.unpackbits(cs.encode_frames(fs, rate, msg), axis=1).astype(np.float32)
+    R = ci["k_ldpc"] / ci["n_ldpc"]
+    ebn0 = 10 ** ((2.0 + 5.0 * (R - 0.5)) / 10)
+    sigma = np.sqrt(1 / (2 * R * ebn0))
+    y = (1 - 2 * bits) + sigma * rng.standard_normal(bits.shape).astype(np.float32)
+    llr = np.clip(np.rint(y * 2 / sigma ** 2 * 4), -32768, 32767).astype(np.int16)
+    T = 30
+    ho, to = O.ldpc_decode(fs, rate, llr, T, nthreads=os.cpu_count() or 8)
+    assert (to >= 0).sum() >= B // 2  # the recipe decodes
+    s = torch.cuda.current_stream()
+    h = torch.zeros((B, ci["k_ldpc"] // 8), dtype=torch.uint8, device="cuda")
+    t = torch.zeros(B, dtype=torch.int32, device="cuda")
+    dec = rg.decoder(fs, rate, T, B)
+    try:
+        dec.launch(torch.from_numpy(llr).cuda(), B, h, t, s)
+        torch.cuda.synchronize()
+    finally:
+        dec.close()
+    hr, tr = h.cpu().numpy(), t.cpu().numpy()
+    conv = (tr >= 0) & (to >= 0)
+    bad = np.nonzero(conv & (hr != ho).any(axis=1))[0]
+    assert len(bad) == 0, f"converged frames {bad[:8]} decode to different bits"
+    assert conv.sum() >= B // 4
+    print(f"fs {fs} rate {rate}: converged ref {(tr >= 0).sum()} oracle {(to >= 0).sum()} both {conv.sum()}, "
+          f"trials identical {(tr == to).sum()} of {B}")
