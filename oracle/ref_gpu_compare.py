@@ -363,6 +363,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--no-fer", action="store_true", help="skip the frame-error-rate comparison")
     ap.add_argument("--fer-only", action="store_true", help="run the frame-error-rate comparison alone")
+    ap.add_argument("--fer-points", default="",
+                    help="frame-error-rate points as MODCOD:framesize:EsN0:frames, comma-separated (default: "
+                         "near the waterfall of C1's and C2's codes)")
     ap.add_argument("--profile-case", action="store_true",
                     help="only two launches of each decoder on the headline batch (for an ncu capture)")
     args = ap.parse_args()
@@ -377,8 +380,11 @@ def main():
     if args.profile_case:
         profile_case(torch, cs, E, O, rg)
         return
+    points = FER_POINTS
+    if args.fer_points:
+        points = [(m, int(f), float(e), int(n)) for m, f, e, n in (x.split(":") for x in args.fer_points.split(","))]
     if args.fer_only:
-        line = json.dumps({"gpu": torch.cuda.get_device_name(0), "fer": fer_section(torch, cs, rg)})
+        line = json.dumps({"gpu": torch.cuda.get_device_name(0), "fer": fer_section(torch, cs, rg, points)})
         print(line)
         if args.out:
             with open(args.out, "w") as f:
@@ -391,7 +397,7 @@ def main():
     res["mixed"] = mixed_section(torch, cs, O, rg, args.steps, args.warmup)
     print(json.dumps(res["mixed"]), file=sys.stderr)
     if not args.no_fer:
-        res["fer"] = fer_section(torch, cs, rg)
+        res["fer"] = fer_section(torch, cs, rg, points)
     line = json.dumps(res)
     print(line)
     if args.out:
