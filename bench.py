@@ -290,7 +290,62 @@ def reference_arm(args, wl):
                              "sample": f"{n} frames of the workload's first batch per step, demap + decode + BCH "
                                        f"(the reference ships no CPU decoder: C restatement of its algorithm)"},
             "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if wl is WORKLOAD or wl["name"] == WORKLOAD["name"]:
+        line["reference_gpu_kernels"] = reference_gpu_leg(args, wl, gen, nb)
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_leg(args, wl, gen, nb):
+    """The reference's own demap and decoder kernels (compiled unchanged into
+    oracle/_ref cubins, launched by oracle/ref_gpu.c as its host classes launch
+    them) on the workload's batches from the oracle's encoder and mapper: one
+    demap + decode per batch on one stream, inputs cycled over batches larger
+    than the L2, CUDA events.  Loads no library of this project.  Reported
+    beside the CPU line, not as its value; {"unavailable": why} where the
+    cubins or a GPU are missing."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device"}
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib as O
+        rg = O.RefGpu()
+        mi = O.modcod(wl["mod"], wl["rate"], wl["fs"])
+        ci, _, bufs, n0, gain = make_traffic(wl, nb, gen)
+        B, T = wl["frames"], wl["max_trials"]
+        g = O.capped_llr_gain(mi, gain)
+        pts = mi["points"]
+        d_re = torch.from_numpy(np.ascontiguousarray(pts.real, np.float32)).cuda()
+        d_im = torch.from_numpy(np.ascontiguousarray(pts.imag, np.float32)).cuda()
+        d_sym = [torch.from_numpy(b).cuda() for b in bufs]
+        llr = torch.zeros((B, mi["fecframe_len"]), dtype=torch.int16, device="cuda")
+        hard = torch.zeros((B, ci["k_ldpc"] // 8), dtype=torch.uint8, device="cuda")
+        res = torch.zeros(B, dtype=torch.int32, device="cuda")
+        dec = rg.decoder(wl["fs"], wl["rate"], T, B)
+        s = torch.cuda.current_stream()
+
+        def step(i):
+            rg.demap(d_sym[i % nb], llr, d_re, d_im, mi, n0, g, B, s)
+            dec.launch(llr, B, hard, res, s)
+
+        for i in range(args.warmup):
+            step(i)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for i in range(args.steps):
+            step(i)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        tr = res.cpu().numpy()
+        dec.close()
+        return {"value": B * ci["k_ldpc"] / (ms * 1e6), "unit": "Gbit/s", "ms_per_step": ms,
+                "frames_failed": int((tr < 0).sum()), "steps": args.steps, "warmup": args.warmup,
+                "kind": "the reference's demapper_kernel.cu and ldpc_decode_kernel.cu compiled unchanged "
+                        "(sm_103 cubins), one demap + decode launch per batch on one stream, no BCH"}
+    except Exception as e:  # the CPU line stands without it
+        return {"unavailable": f"{type(e).__name__}: {e}"[:300]}
 
 
 # The other configurations, run after the headline's timed region as
